@@ -1,0 +1,297 @@
+/*
+ * omc_gpu.h -- C ABI of the GB300 photon/electron voxel transport engine.
+ *
+ * The reference (edoerner/ompMC) is a C library whose "API" is the EGS
+ * user-code contract: a front end (ucodes/omc_dosxyz/omc_dosxyz.c,
+ * ucodes/omc_matrad/omc_matrad.c) parses a key/value input file, builds the
+ * interaction tables with initMediaData() (src/ompmc.c:5450), and then runs
+ *
+ *     for batch: #pragma omp parallel for  { initHistory(); shower(); }
+ *
+ * (omc_dosxyz.c:1237-1263, omc_matrad.c:1389-1414) with per-step host
+ * callbacks howfar/hownear/ausgab (src/ompmc.h:37-39).  Per-step host
+ * callbacks cannot cross to a GPU, so the drop-in boundary here is the
+ * "run N histories" call: omc_engine_run() replaces that batch/history loop,
+ * and the geometry, source and scoring semantics of howfar/hownear/ausgab/
+ * initHistory live on the device.  Everything else keeps the reference's
+ * input formats and meaning: the .inp key/value file, .egsphant phantoms,
+ * spectrum files, pegs4 media, XCOM cross sections, pgs4form form factors,
+ * msnew.data and spinms.data, and the .3ddose output.
+ *
+ * Conventions
+ *  - Plain C types only; every array is caller-visible host memory unless a
+ *    function says "device".
+ *  - Region index irl = 1 + ix + iy*nx + iz*nx*ny, irl = 0 is outside the
+ *    phantom (omc_dosxyz.c:205-207, 735).  Per-region arrays have
+ *    nx*ny*nz + 1 entries.
+ *  - Every function returns omc_status; the reference's printf+exit paths
+ *    become error codes with a message in omc_last_error().
+ *  - Engines are not thread safe; use one engine per host thread.
+ */
+#ifndef OMC_GPU_H
+#define OMC_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Table dimensions, identical to the reference (src/ompmc.h). */
+#define OMC_MXMED 9          /* media per problem          ompmc.h:358 */
+#define OMC_MXELEMENT 50     /* elements read from data     ompmc.h:359 */
+#define OMC_MXGE 2000        /* photon log-energy bins      ompmc.h:102 */
+#define OMC_MXEKE 500        /* electron log-energy bins    ompmc.h:360 */
+#define OMC_MXRAYFF 100      /* Rayleigh form-factor grid   ompmc.h:130 */
+#define OMC_RAYCDFSIZE 100   /* Rayleigh CDF bins           ompmc.h:131 */
+#define OMC_MXE_SPIN 15      /*                             ompmc.h:257 */
+#define OMC_MXE_SPIN1 31     /* 2*MXE_SPIN+1                ompmc.h:258 */
+#define OMC_MXQ_SPIN 15      /*                             ompmc.h:259 */
+#define OMC_MXU_SPIN 31      /*                             ompmc.h:260 */
+#define OMC_MXL_MS 63        /* msnew lambda grid           ompmc.h:292 */
+#define OMC_MXQ_MS 7         /* msnew q grid                ompmc.h:293 */
+#define OMC_MXU_MS 31        /* msnew u grid                ompmc.h:294 */
+#define OMC_INVDIM 1000      /* spectrum inverse-CDF bins   omc_dosxyz.c:340 */
+#define OMC_MXEBIN 200       /* spectrum bins               omc_dosxyz.c:339 */
+#define OMC_NAME_LEN 64
+
+typedef enum omc_status {
+    OMC_OK = 0,
+    OMC_ERR_ARG = 1,      /* invalid argument                              */
+    OMC_ERR_IO = 2,       /* file missing or unreadable                    */
+    OMC_ERR_INPUT = 3,    /* required .inp key missing or malformed        */
+    OMC_ERR_MEDIA = 4,    /* medium not found in the pegs4 file            */
+    OMC_ERR_FORMAT = 5,   /* data file does not follow its format          */
+    OMC_ERR_NOMEM = 6,    /* host or device allocation failed              */
+    OMC_ERR_CUDA = 7,     /* CUDA runtime error                            */
+    OMC_ERR_STACK = 8,    /* particle stack overflow on the device         */
+    OMC_ERR_LIMIT = 9,    /* a bounded device loop hit its iteration limit */
+    OMC_ERR_STATE = 10    /* call out of order (e.g. run before load)      */
+} omc_status;
+
+const char *omc_status_string(omc_status s);
+/* Message of the most recent failing call on this host thread. */
+const char *omc_last_error(void);
+
+/* ------------------------------------------------------------------------
+ * Input file.  Replaces parseInputFile/getInputValue
+ * (src/omc_utilities.c:63-123): "key = value" lines, any line containing '#'
+ * or only white space is skipped, keys match by SUBSTRING, first match wins.
+ * ---------------------------------------------------------------------- */
+typedef struct omc_input omc_input;
+
+/* Parses "<path>.inp" (the ".inp" extension is appended, as the reference). */
+omc_status omc_input_parse(const char *path_without_ext, omc_input **out);
+/* Parses the same format from a string. */
+omc_status omc_input_from_string(const char *text, omc_input **out);
+/* 1 and the value copied to dest if found, 0 otherwise. */
+int omc_input_get(const omc_input *in, const char *key, char *dest, size_t cap);
+void omc_input_free(omc_input *in);
+
+/* ------------------------------------------------------------------------
+ * Phantom.  Replaces initPhantom (omc_dosxyz.c:62-175) and the MATLAB-array
+ * variant of omc_matrad (omc_matrad.c:269-342).
+ * ---------------------------------------------------------------------- */
+typedef struct omc_phantom {
+    int nmed;
+    char med_names[OMC_MXMED][OMC_NAME_LEN];
+    int nx, ny, nz;
+    double *xbounds; /* nx+1 */
+    double *ybounds; /* ny+1 */
+    double *zbounds; /* nz+1 */
+    int *med_index;  /* nx*ny*nz, egsphant medium number (1-based, 0 = vacuum) */
+    double *density; /* nx*ny*nz, g/cm^3 */
+} omc_phantom;
+
+omc_status omc_phantom_read(const char *egsphant_path, omc_phantom **out);
+omc_status omc_phantom_create(int nmed, const char *const *med_names, int nx,
+                              int ny, int nz, const double *xbounds,
+                              const double *ybounds, const double *zbounds,
+                              const int *med_index, const double *density,
+                              omc_phantom **out);
+omc_status omc_phantom_write(const omc_phantom *ph, const char *egsphant_path);
+void omc_phantom_free(omc_phantom *ph);
+
+/* ------------------------------------------------------------------------
+ * Media and interaction tables.  Replaces initMediaData (ompmc.c:5450):
+ * readPegsFile (:5489), initPhotonData (:471), initRayleighData (:820),
+ * initPairData (:1189), initMscatData (:3282) with initSpinData (:2376).
+ * Field names and index layouts are the reference's globals photon_data,
+ * rayleigh_data, pair_data, electron_data, spin_data, mscat_data, pegs_data
+ * (ompmc.h:105-404), so values compare one to one.
+ * Reads the "pegs file", "pgs4form file" and "data folder" keys.
+ * ---------------------------------------------------------------------- */
+typedef struct omc_tables {
+    int nmed;
+    char names[OMC_MXMED][OMC_NAME_LEN];
+    /* pegs_data */
+    int ne[OMC_MXMED], meke[OMC_MXMED];
+    double rho[OMC_MXMED], rlc[OMC_MXMED], ae[OMC_MXMED], ap[OMC_MXMED];
+    double ue[OMC_MXMED], up[OMC_MXMED], te[OMC_MXMED], thmoll[OMC_MXMED];
+    double pegs_delcm[OMC_MXMED];
+    /* photon_data: ge0/ge1 [nmed]; the rest [nmed*MXGE] */
+    double *ge0, *ge1;
+    double *gmfp0, *gmfp1, *gbr10, *gbr11, *gbr20, *gbr21, *cohe0, *cohe1;
+    /* rayleigh_data: [nmed*MXRAYFF] except pmax [nmed*MXGE] */
+    double *xgrid, *fcum, *b_array, *c_array, *pmax0, *pmax1;
+    int *i_array;
+    /* pair_data: dl* [nmed*8], the rest [nmed] */
+    double *dl1, *dl2, *dl3, *dl4, *dl5, *dl6;
+    double *bpar0, *bpar1, *delcm, *zbrang;
+    /* electron_data: [nmed*MXEKE] unless noted */
+    double *esig0, *esig1, *psig0, *psig1;
+    double *ededx0, *ededx1, *pdedx0, *pdedx1;
+    double *ebr10, *ebr11, *pbr10, *pbr11, *pbr20, *pbr21;
+    double *tmxs0, *tmxs1, *blcce0, *blcce1;
+    double *etae_ms0, *etae_ms1, *etap_ms0, *etap_ms1;
+    double *q1ce_ms0, *q1ce_ms1, *q1cp_ms0, *q1cp_ms1;
+    double *q2ce_ms0, *q2ce_ms1, *q2cp_ms0, *q2cp_ms1;
+    double *e_array;
+    double *range_ep;       /* [2*nmed*MXEKE], [qel][imed][i] */
+    double *eke0, *eke1;    /* [nmed] */
+    int *sig_ismonotone;    /* [2*nmed], [qel][imed] */
+    double *esig_e, *psig_e, *xcc, *blcc, *expeke1; /* [nmed] */
+    /* spin_data */
+    double b2spin_min, dbeta2i, espml, dleneri, dqq1i;
+    double *spin_rej; /* [nmed][2][MXE_SPIN1+1][MXQ_SPIN+1][MXU_SPIN+1] */
+    /* mscat_data: [(MXL_MS+1)*(MXQ_MS+1)*(MXU_MS+1)] */
+    double *ums, *fms, *wms;
+    int *ims;
+    double dllambi, dqmsi;
+} omc_tables;
+
+/* Builds tables for the media named in med_names (nmed entries, the
+ * phantom's media list, in that order). */
+omc_status omc_tables_build(const omc_input *in, int nmed,
+                            const char (*med_names)[OMC_NAME_LEN],
+                            omc_tables **out);
+void omc_tables_free(omc_tables *t);
+/* Writes every table in the "OMCT" record format used by the test oracle
+ * (4-byte magic, then {u32 name length, name, u8 'd'|'i', u64 n, data}). */
+omc_status omc_tables_dump(const omc_tables *t, const char *path);
+
+/* ------------------------------------------------------------------------
+ * Regions.  Replaces initRegions (omc_dosxyz.c:890-962): per region medium
+ * (egsphant index - 1, -1 = vacuum), density ratio rhof, pcut, ecut.
+ * Reads "global ecut" and "global pcut".  Where the reference leaves ecut
+ * unset (global ecut below the pegs AE, omc_dosxyz.c:951-957) the pegs AE is
+ * used, which is what its warning message announces.
+ * ---------------------------------------------------------------------- */
+typedef struct omc_regions {
+    int nreg; /* nx*ny*nz + 1 */
+    int *med;
+    double *rhof, *pcut, *ecut;
+} omc_regions;
+
+omc_status omc_regions_build(const omc_input *in, const omc_phantom *ph,
+                             const omc_tables *t, omc_regions **out);
+void omc_regions_free(omc_regions *r);
+
+/* ------------------------------------------------------------------------
+ * Source.  Replaces initSource (omc_dosxyz.c:368-632): a point source at
+ * distance "ssd" above a collimated rectangle on the phantom's z = zmin
+ * face, monoenergetic ("mono energy") or from a spectrum file ("spectrum
+ * file", which takes precedence), charge -1/0/+1.  Beamlet sources of
+ * omc_matrad (omc_matrad.c:502-760, 1084-1254) use omc_beamlets below.
+ * ---------------------------------------------------------------------- */
+typedef struct omc_source {
+    int spectrum; /* 0 mono, 1 spectrum */
+    int charge;
+    double energy;
+    double deltak; /* INVDIM */
+    double cdfinv1[OMC_INVDIM], cdfinv2[OMC_INVDIM];
+    double ssd;
+    double xinl, xinu, yinl, yinu, xsize, ysize;
+    int ixinl, ixinu, iyinl, iyinu;
+} omc_source;
+
+omc_status omc_source_build(const omc_input *in, const omc_phantom *ph,
+                            omc_source **out);
+void omc_source_free(omc_source *s);
+
+/* ------------------------------------------------------------------------
+ * Scoring output.  Replaces accumulateResults/outputResults
+ * (omc_dosxyz.c:719-886): batch mean and batch relative uncertainty, energy
+ * to Gy by 1.602e-10/(rho*V*N), zero dose where density < 0.044.
+ * dose/unc have nx*ny*nz+1 entries in region order (index 0 unused).
+ * ---------------------------------------------------------------------- */
+omc_status omc_accumulate_results(const omc_phantom *ph,
+                                  const double *accum_endep,
+                                  const double *accum_endep2, int iout,
+                                  long long nhist, int nbatch, double *dose,
+                                  double *unc);
+omc_status omc_write_3ddose(const char *path, const omc_phantom *ph,
+                            const double *dose, const double *unc);
+
+/* ------------------------------------------------------------------------
+ * Transport engine (GB300).  One engine owns one CUDA device context
+ * slot, its resident tables, geometry and RANMAR streams.
+ * ---------------------------------------------------------------------- */
+typedef struct omc_engine omc_engine;
+
+typedef enum omc_precision {
+    OMC_FP64 = 0, /* FP64 transport and tallies (the reference's arithmetic) */
+    OMC_FP32 = 1  /* FP32 transport arithmetic, FP64 tallies and balances   */
+} omc_precision;
+
+typedef struct omc_run_config {
+    long long nperbatch; /* histories per batch                           */
+    int nbatch;          /* statistical batches (omc_dosxyz.c:1214-1225)  */
+    int ixx, jxx;        /* "rng seeds"; lane k uses the k-th seed pair   */
+    int nsplit;          /* "nsplit" photon splitting (ompmc.c:5964)      */
+    int precision;       /* omc_precision                                 */
+    int nlanes;          /* concurrent histories; 0 = sized to the GPU    */
+    int stack_depth;     /* per-lane particle stack; 0 = default          */
+    int serial;          /* 1 = one lane, one stream: the reference's
+                            serial build, history order included          */
+} omc_run_config;
+
+typedef struct omc_run_stats {
+    double ensrc;          /* source kinetic energy, FP64 (score.ensrc)    */
+    double transport_ms;   /* device time of the batch loop               */
+    long long histories;   /* histories transported                       */
+    long long steps;       /* particle events processed                   */
+    int max_stack;         /* deepest per-lane stack seen                 */
+    int error_flags;       /* OR of device error bits (0 = clean)         */
+} omc_run_stats;
+
+omc_status omc_engine_create(int device, omc_engine **out);
+void omc_engine_destroy(omc_engine *e);
+/* Upload tables (kept resident in FP64 and FP32 layouts). */
+omc_status omc_engine_set_tables(omc_engine *e, const omc_tables *t);
+/* Upload the voxel geometry and per-region data. */
+omc_status omc_engine_set_geometry(omc_engine *e, const omc_phantom *ph,
+                                   const omc_regions *r);
+omc_status omc_engine_set_source(omc_engine *e, const omc_source *s);
+
+/* Runs nbatch batches of nperbatch histories (replaces omc_dosxyz.c:
+ * 1237-1263).  accum_endep/accum_endep2 (host, nreg entries each, may be
+ * NULL) receive the sum over batches of the batch energy deposit and of its
+ * square, exactly the reference's score.accum_endep/accum_endep2 before
+ * accumulateResults(). */
+omc_status omc_engine_run(omc_engine *e, const omc_run_config *cfg,
+                          double *accum_endep, double *accum_endep2,
+                          omc_run_stats *stats);
+/* Same, leaving the tallies on the device; returns device pointers valid
+ * until the next run (for resident pipelines and benchmarks). */
+omc_status omc_engine_run_resident(omc_engine *e, const omc_run_config *cfg,
+                                   const double **d_accum_endep,
+                                   const double **d_accum_endep2,
+                                   omc_run_stats *stats);
+
+/* RANMAR streams on the device (bit-exact with initRandom/setRandom,
+ * omc_random.c:58-187).  Stream k is seeded with the k-th pair of the
+ * sequence (ixx, jxx), (ixx, jxx+1), ..., (the reference's per-thread
+ * seeding, omc_random.c:72, continued past jxx = 31328 into ixx+1).
+ * out[k*n + i] = 24-bit integer of the i-th number of stream k. */
+omc_status omc_gpu_ranmar(int device, int ixx, int jxx, int nstreams,
+                          long long n, int32_t *out);
+
+/* Seed pair of stream k under the rule above (host helper). */
+void omc_stream_seeds(int ixx, int jxx, long long k, int *ixx_k, int *jxx_k);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OMC_GPU_H */

@@ -1,0 +1,130 @@
+"""ctypes binding of the C ABI declared in include/omc_gpu.h.
+
+The shared library ``ompmc_gb300/lib/libompmc_gb300.so`` holds the host
+library (input, phantom, tables, regions, source, scoring) and the CUDA
+transport engine.  It is built in-tree by :mod:`ompmc_gb300.build`.  There
+is no fallback: if the library is missing, importing a symbol raises.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libompmc_gb300.so")
+
+MXMED = 9
+NAME_LEN = 64
+INVDIM = 1000
+
+
+class OmcError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"{message} (status {status})")
+        self.status = status
+
+
+class Phantom_t(C.Structure):
+    _fields_ = [("nmed", C.c_int), ("med_names", (C.c_char * NAME_LEN) * MXMED),
+                ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+                ("xbounds", C.POINTER(C.c_double)), ("ybounds", C.POINTER(C.c_double)),
+                ("zbounds", C.POINTER(C.c_double)), ("med_index", C.POINTER(C.c_int)),
+                ("density", C.POINTER(C.c_double))]
+
+
+class Regions_t(C.Structure):
+    _fields_ = [("nreg", C.c_int), ("med", C.POINTER(C.c_int)), ("rhof", C.POINTER(C.c_double)),
+                ("pcut", C.POINTER(C.c_double)), ("ecut", C.POINTER(C.c_double))]
+
+
+class Source_t(C.Structure):
+    _fields_ = [("spectrum", C.c_int), ("charge", C.c_int), ("energy", C.c_double),
+                ("deltak", C.c_double), ("cdfinv1", C.c_double * INVDIM),
+                ("cdfinv2", C.c_double * INVDIM), ("ssd", C.c_double),
+                ("xinl", C.c_double), ("xinu", C.c_double), ("yinl", C.c_double),
+                ("yinu", C.c_double), ("xsize", C.c_double), ("ysize", C.c_double),
+                ("ixinl", C.c_int), ("ixinu", C.c_int), ("iyinl", C.c_int), ("iyinu", C.c_int)]
+
+
+class TablesHead_t(C.Structure):
+    """Leading fields of omc_tables (the rest is only used natively)."""
+    _fields_ = [("nmed", C.c_int), ("names", (C.c_char * NAME_LEN) * MXMED),
+                ("ne", C.c_int * MXMED), ("meke", C.c_int * MXMED),
+                ("rho", C.c_double * MXMED), ("rlc", C.c_double * MXMED),
+                ("ae", C.c_double * MXMED), ("ap", C.c_double * MXMED),
+                ("ue", C.c_double * MXMED), ("up", C.c_double * MXMED),
+                ("te", C.c_double * MXMED), ("thmoll", C.c_double * MXMED)]
+
+
+class RunConfig_t(C.Structure):
+    _fields_ = [("nperbatch", C.c_longlong), ("nbatch", C.c_int), ("ixx", C.c_int), ("jxx", C.c_int),
+                ("nsplit", C.c_int), ("precision", C.c_int), ("nlanes", C.c_int),
+                ("stack_depth", C.c_int), ("serial", C.c_int)]
+
+
+class RunStats_t(C.Structure):
+    _fields_ = [("ensrc", C.c_double), ("transport_ms", C.c_double), ("histories", C.c_longlong),
+                ("steps", C.c_longlong), ("max_stack", C.c_int), ("error_flags", C.c_int)]
+
+
+_lib = None
+
+
+def lib(path: str | None = None):
+    """Load (once) and return the native library."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or os.environ.get("OMC_LIB", LIB_PATH)
+    if not os.path.exists(path):
+        raise OmcError(-1, f"native library not built: {path} (run ompmc_gb300.build.build())")
+    L = C.CDLL(path)
+    vp, pp = C.c_void_p, C.POINTER
+    sig = {
+        "omc_last_error": ([], C.c_char_p),
+        "omc_status_string": ([C.c_int], C.c_char_p),
+        "omc_input_parse": ([C.c_char_p, pp(vp)], C.c_int),
+        "omc_input_from_string": ([C.c_char_p, pp(vp)], C.c_int),
+        "omc_input_get": ([vp, C.c_char_p, C.c_char_p, C.c_size_t], C.c_int),
+        "omc_input_free": ([vp], None),
+        "omc_phantom_read": ([C.c_char_p, pp(pp(Phantom_t))], C.c_int),
+        "omc_phantom_create": ([C.c_int, pp(C.c_char_p), C.c_int, C.c_int, C.c_int, pp(C.c_double),
+                                pp(C.c_double), pp(C.c_double), pp(C.c_int), pp(C.c_double),
+                                pp(pp(Phantom_t))], C.c_int),
+        "omc_phantom_write": ([pp(Phantom_t), C.c_char_p], C.c_int),
+        "omc_phantom_free": ([pp(Phantom_t)], None),
+        "omc_tables_build": ([vp, C.c_int, vp, pp(vp)], C.c_int),
+        "omc_tables_free": ([vp], None),
+        "omc_tables_dump": ([vp, C.c_char_p], C.c_int),
+        "omc_regions_build": ([vp, pp(Phantom_t), vp, pp(pp(Regions_t))], C.c_int),
+        "omc_regions_free": ([pp(Regions_t)], None),
+        "omc_source_build": ([vp, pp(Phantom_t), pp(pp(Source_t))], C.c_int),
+        "omc_source_free": ([pp(Source_t)], None),
+        "omc_accumulate_results": ([pp(Phantom_t), pp(C.c_double), pp(C.c_double), C.c_int, C.c_longlong,
+                                    C.c_int, pp(C.c_double), pp(C.c_double)], C.c_int),
+        "omc_write_3ddose": ([C.c_char_p, pp(Phantom_t), pp(C.c_double), pp(C.c_double)], C.c_int),
+        "omc_engine_create": ([C.c_int, pp(vp)], C.c_int),
+        "omc_engine_destroy": ([vp], None),
+        "omc_engine_set_tables": ([vp, vp], C.c_int),
+        "omc_engine_set_geometry": ([vp, pp(Phantom_t), pp(Regions_t)], C.c_int),
+        "omc_engine_set_source": ([vp, pp(Source_t)], C.c_int),
+        "omc_engine_run": ([vp, pp(RunConfig_t), pp(C.c_double), pp(C.c_double), pp(RunStats_t)], C.c_int),
+        "omc_engine_run_resident": ([vp, pp(RunConfig_t), pp(vp), pp(vp), pp(RunStats_t)], C.c_int),
+        "omc_gpu_ranmar": ([C.c_int, C.c_int, C.c_int, C.c_int, C.c_longlong, pp(C.c_int32)], C.c_int),
+        "omc_stream_seeds": ([C.c_int, C.c_int, C.c_longlong, pp(C.c_int), pp(C.c_int)], None),
+    }
+    for name, (args, res) in sig.items():
+        if not hasattr(L, name):
+            continue
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def check(status: int):
+    if status != 0:
+        L = lib()
+        raise OmcError(status, L.omc_last_error().decode(errors="replace"))

@@ -1,0 +1,233 @@
+"""Python mirror of the omc_dosxyz front end over the C ABI.
+
+``Problem`` runs the reference's initialisation chain (parseInputFile,
+initPhantom, initMediaData, initSource, initRegions, initVrt;
+ucodes/omc_dosxyz/omc_dosxyz.c:1155-1179) through the native host library.
+``Engine`` is the GPU transport that replaces the batch/history loop
+(omc_dosxyz.c:1237-1263).  ``Problem.dose()`` and ``write_3ddose`` are
+accumulateResults/outputResults (:719-886).
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _native as N
+from ._native import check
+
+FP64, FP32 = 0, 1
+
+
+def _dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Input:
+    def __init__(self, path_without_ext: str | None = None, text: str | None = None):
+        L = N.lib()
+        self._h = C.c_void_p()
+        if text is not None:
+            check(L.omc_input_from_string(text.encode(), C.byref(self._h)))
+        else:
+            check(L.omc_input_parse(path_without_ext.encode(), C.byref(self._h)))
+
+    def get(self, key: str):
+        buf = C.create_string_buffer(1024)
+        if N.lib().omc_input_get(self._h, key.encode(), buf, 1024):
+            return buf.value.decode()
+        return None
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            N.lib().omc_input_free(self._h)
+            self._h = None
+
+
+class Phantom:
+    def __init__(self, ptr):
+        self._p = ptr
+
+    @classmethod
+    def read(cls, path: str):
+        p = C.POINTER(N.Phantom_t)()
+        check(N.lib().omc_phantom_read(path.encode(), C.byref(p)))
+        return cls(p)
+
+    @classmethod
+    def from_arrays(cls, media, xb, yb, zb, med, rho):
+        """med: [nz,ny,nx] 1-based medium numbers; rho: densities."""
+        med = np.ascontiguousarray(med, dtype=np.int32)
+        rho = np.ascontiguousarray(rho, dtype=np.float64)
+        nz, ny, nx = med.shape
+        names = (C.c_char_p * len(media))(*[m.encode() for m in media])
+        xb, yb, zb = (np.ascontiguousarray(b, dtype=np.float64) for b in (xb, yb, zb))
+        p = C.POINTER(N.Phantom_t)()
+        check(N.lib().omc_phantom_create(len(media), names, nx, ny, nz, _dptr(xb), _dptr(yb), _dptr(zb),
+                                          med.ctypes.data_as(C.POINTER(C.c_int)), _dptr(rho), C.byref(p)))
+        return cls(p)
+
+    @property
+    def s(self):
+        return self._p.contents
+
+    @property
+    def shape(self):
+        s = self.s
+        return (s.nz, s.ny, s.nx)
+
+    @property
+    def nreg(self):
+        s = self.s
+        return s.nx * s.ny * s.nz + 1
+
+    @property
+    def media(self):
+        s = self.s
+        return [s.med_names[i].value.decode() for i in range(s.nmed)]
+
+    def density(self):
+        s = self.s
+        return np.ctypeslib.as_array(s.density, shape=(s.nz * s.ny * s.nx,)).reshape(self.shape).copy()
+
+    def write(self, path):
+        check(N.lib().omc_phantom_write(self._p, path.encode()))
+
+    def __del__(self):
+        if getattr(self, "_p", None):
+            N.lib().omc_phantom_free(self._p)
+            self._p = None
+
+
+class Problem:
+    """Host-side state of one dose job, built from a .inp file."""
+
+    def __init__(self, inp: Input, phantom: Phantom | None = None):
+        L = N.lib()
+        self.input = inp
+        if phantom is None:
+            path = inp.get("phantom file")
+            if path is None:
+                raise N.OmcError(3, "Can not find 'phantom file' key on input file.")
+            phantom = Phantom.read("".join(path.split()))
+        self.phantom = phantom
+        ps = phantom.s
+        self.tables = C.c_void_p()
+        check(L.omc_tables_build(inp._h, ps.nmed, C.cast(C.pointer(ps.med_names), C.c_void_p),
+                                 C.byref(self.tables)))
+        self.regions = C.POINTER(N.Regions_t)()
+        check(L.omc_regions_build(inp._h, phantom._p, self.tables, C.byref(self.regions)))
+        self.source = C.POINTER(N.Source_t)()
+        check(L.omc_source_build(inp._h, phantom._p, C.byref(self.source)))
+        g = lambda k, d: int(inp.get(k)) if inp.get(k) is not None else d
+        self.nsplit = g("nsplit", 1)
+        ncase, nbatch = g("ncase", 0), g("nbatch", 1)
+        if nbatch > 0 and ncase // nbatch == 0:
+            ncase = nbatch
+        self.nbatch = nbatch
+        self.nperbatch = ncase // nbatch if nbatch > 0 else 0
+        seeds = (inp.get("rng seeds") or "97 33").split()
+        self.seeds = (int(seeds[0]), int(seeds[1]))
+
+    @classmethod
+    def from_file(cls, path_without_ext: str):
+        return cls(Input(path_without_ext))
+
+    @property
+    def nreg(self):
+        return self.phantom.nreg
+
+    def tables_head(self):
+        return C.cast(self.tables, C.POINTER(N.TablesHead_t)).contents
+
+    def dump_tables(self, path):
+        check(N.lib().omc_tables_dump(self.tables, path.encode()))
+
+    def dose(self, accum_endep, accum_endep2, nperbatch=None, nbatch=None, iout=1):
+        """Batch mean dose (Gy per history) and relative uncertainty."""
+        nperbatch = self.nperbatch if nperbatch is None else nperbatch
+        nbatch = self.nbatch if nbatch is None else nbatch
+        a = np.ascontiguousarray(accum_endep, dtype=np.float64)
+        a2 = np.ascontiguousarray(accum_endep2, dtype=np.float64)
+        dose = np.zeros(self.nreg)
+        unc = np.zeros(self.nreg)
+        check(N.lib().omc_accumulate_results(self.phantom._p, _dptr(a), _dptr(a2), iout, nperbatch, nbatch,
+                                             _dptr(dose), _dptr(unc)))
+        return dose, unc
+
+    def write_3ddose(self, path, dose, unc):
+        check(N.lib().omc_write_3ddose(path.encode(), self.phantom._p, _dptr(dose), _dptr(unc)))
+
+    def __del__(self):
+        L = N.lib()
+        if getattr(self, "source", None):
+            L.omc_source_free(self.source)
+            self.source = None
+        if getattr(self, "regions", None):
+            L.omc_regions_free(self.regions)
+            self.regions = None
+        if getattr(self, "tables", None):
+            L.omc_tables_free(self.tables)
+            self.tables = None
+
+
+class Engine:
+    """GB300 transport engine (omc_engine_*)."""
+
+    def __init__(self, device: int = 0):
+        self._h = C.c_void_p()
+        check(N.lib().omc_engine_create(device, C.byref(self._h)))
+        self._problem = None
+
+    def load(self, problem: Problem):
+        L = N.lib()
+        check(L.omc_engine_set_tables(self._h, problem.tables))
+        check(L.omc_engine_set_geometry(self._h, problem.phantom._p, problem.regions))
+        check(L.omc_engine_set_source(self._h, problem.source))
+        self._problem = problem
+        return self
+
+    @staticmethod
+    def config(nperbatch, nbatch, seeds=(97, 33), nsplit=1, precision=FP64, nlanes=0, stack_depth=0, serial=0):
+        return N.RunConfig_t(int(nperbatch), int(nbatch), int(seeds[0]), int(seeds[1]), int(nsplit),
+                             int(precision), int(nlanes), int(stack_depth), int(serial))
+
+    def run(self, nperbatch=None, nbatch=None, seeds=None, nsplit=None, precision=FP64, nlanes=0,
+            stack_depth=0, serial=0):
+        p = self._problem
+        cfg = self.config(p.nperbatch if nperbatch is None else nperbatch, p.nbatch if nbatch is None else nbatch,
+                          p.seeds if seeds is None else seeds, p.nsplit if nsplit is None else nsplit,
+                          precision, nlanes, stack_depth, serial)
+        a = np.zeros(p.nreg)
+        a2 = np.zeros(p.nreg)
+        st = N.RunStats_t()
+        check(N.lib().omc_engine_run(self._h, C.byref(cfg), _dptr(a), _dptr(a2), C.byref(st)))
+        return a, a2, st
+
+    def run_resident(self, cfg):
+        d1, d2 = C.c_void_p(), C.c_void_p()
+        st = N.RunStats_t()
+        check(N.lib().omc_engine_run_resident(self._h, C.byref(cfg), C.byref(d1), C.byref(d2), C.byref(st)))
+        return d1.value, d2.value, st
+
+    def close(self):
+        if getattr(self, "_h", None):
+            N.lib().omc_engine_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+def gpu_ranmar(ixx, jxx, nstreams, n, device=0):
+    out = np.zeros((nstreams, n), dtype=np.int32)
+    check(N.lib().omc_gpu_ranmar(device, ixx, jxx, nstreams, n, out.ctypes.data_as(C.POINTER(C.c_int32))))
+    return out
+
+
+def stream_seeds(ixx, jxx, k):
+    a, b = C.c_int(), C.c_int()
+    N.lib().omc_stream_seeds(ixx, jxx, k, C.byref(a), C.byref(b))
+    return a.value, b.value
