@@ -10,9 +10,10 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import platform
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "lib", "libompmc_gb300.so")
+LIB_PATH = os.path.join(HERE, "lib", platform.machine(), "libompmc_gb300.so")
 
 MXMED = 9
 NAME_LEN = 64

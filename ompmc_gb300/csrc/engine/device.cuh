@@ -1,0 +1,179 @@
+// Device-side building blocks of the transport engine: precision traits,
+// RANMAR streams, per-lane particle stacks, resident tables and the voxel
+// geometry.  Physics lives in physics.cuh.
+#pragma once
+
+#include <cstdint>
+
+#include "omc_gpu.h"
+
+namespace omcgpu {
+
+constexpr int MXGE = OMC_MXGE;
+constexpr int MXEKE = OMC_MXEKE;
+constexpr int MXRAYFF = OMC_MXRAYFF;
+constexpr int MXE_SPIN = OMC_MXE_SPIN;
+constexpr int MXE_SPIN1 = OMC_MXE_SPIN1;
+constexpr int MXQ_SPIN = OMC_MXQ_SPIN;
+constexpr int MXU_SPIN = OMC_MXU_SPIN;
+constexpr int MXL_MS = OMC_MXL_MS;
+constexpr int MXQ_MS = OMC_MXQ_MS;
+constexpr int MXU_MS = OMC_MXU_MS;
+constexpr int RNG_WORDS = 97;
+
+// Device error bits (omc_run_stats.error_flags).
+enum : unsigned {
+  ERR_STACK = 1u,      // per-lane stack overflow: history dropped
+  ERR_LOOP = 2u,       // a rejection loop hit its iteration cap
+  ERR_EVENTS = 4u,     // a history exceeded the event cap: history dropped
+  ERR_TABLE = 8u       // an interpolation index left its table (clamped)
+};
+
+// Iteration caps of device loops.  The reference's loops end with
+// probability one; the caps only turn a pathological input into an error
+// flag instead of a hung GPU.
+constexpr int kRejectCap = 1 << 20;
+constexpr long long kEventCap = 1ll << 22;
+
+// ---------------------------------------------------------------------------
+// Particles.  dnear is not carried: the reference writes it but never reads
+// it (ompmc.c:4934-4935, 5109, 5254).
+template <typename R>
+struct Particle {
+  R e, x, y, z, u, v, w, wt;
+  int iq, ir;
+};
+
+// ---------------------------------------------------------------------------
+// Tables resident on the device, in the reference's index layout (the
+// arrays of omc_tables), converted to R.
+template <typename R>
+struct Tables {
+  int nmed;
+  // per medium
+  const R *ge0, *ge1, *eke0, *eke1, *xcc, *blcc, *te, *thmoll, *ap;
+  const R *esig_e, *psig_e, *delcm, *zbrang, *bpar0, *bpar1;
+  const int *monotone;  // [2*nmed]
+  // photon [nmed*MXGE]
+  const R *gmfp0, *gmfp1, *gbr10, *gbr11, *gbr20, *gbr21, *cohe0, *cohe1, *pmax0, *pmax1;
+  // rayleigh [MXRAYFF] of medium 0 (see rayleigh())
+  const R *xgrid, *fcum, *b_array, *c_array;
+  const int *i_array;
+  // pair/brems [nmed*8]
+  const R *dl1, *dl2, *dl3, *dl4, *dl5, *dl6;
+  // electron [nmed*MXEKE]
+  const R *esig0, *esig1, *psig0, *psig1, *ededx0, *ededx1, *pdedx0, *pdedx1;
+  const R *ebr10, *ebr11, *pbr10, *pbr11, *pbr20, *pbr21, *tmxs0, *tmxs1, *blcce0, *blcce1;
+  const R *etae0, *etae1, *etap0, *etap1, *q1ce0, *q1ce1, *q1cp0, *q1cp1, *q2ce0, *q2ce1, *q2cp0, *q2cp1;
+  const R *e_array, *range_ep;  // range_ep [2*nmed*MXEKE]
+  const int *meke;              // [nmed]
+  // spin
+  R b2spin_min, dbeta2i, espml, dleneri, dqq1i;
+  const R *spin_rej;
+  // msnew
+  const R *ums, *fms, *wms;
+  const int *ims;
+  R dllambi, dqmsi;
+};
+
+// Voxel geometry and per-region data.
+template <typename R>
+struct Geometry {
+  int nx, ny, nz, nxy;
+  const R *xb, *yb, *zb;
+  const int8_t *med;  // [nreg], -1 vacuum / outside
+  const R *rhof;      // [nreg]
+  const R *ecut_m, *pcut_m;  // per medium (+1 slot for vacuum at index 0)
+};
+
+// Source (initSource, omc_dosxyz.c:368-632) in R.
+template <typename R>
+struct Source {
+  int spectrum, charge;
+  R energy, deltak;
+  const R *cdfinv1, *cdfinv2;  // [INVDIM]
+  R ssd, xinl, yinl, xsize, ysize;
+  int ixinl, iyinl;
+};
+
+template <typename R>
+struct Params {
+  Tables<R> T;
+  Geometry<R> G;
+  Source<R> S;
+  int nsplit;
+  int nlanes;
+  int depth;                 // per-lane stack slots
+  long long nhist;           // histories of this launch
+  unsigned long long *next;  // history counter
+  // per-lane state in HBM
+  int *rng_u;                // [97][nlanes]
+  int *rng_ijc;              // [3][nlanes]
+  R *stk;                    // [8][depth][nlanes]
+  int *stk_key;              // [depth][nlanes]  ir*4 + iq+1
+  // outputs
+  double *endep;             // [nreg] batch tally
+  double *ensrc;             // [1]
+  unsigned long long *events;
+  int *max_np;
+  unsigned *err;
+};
+
+// ---------------------------------------------------------------------------
+// RANMAR (omc_random.c:58-187) with the 97-word state in shared memory,
+// word k of a thread at u[k*stride].  Numbers are produced one at a time;
+// the reference refills blocks of 128 but returns them in the same order.
+struct Ranmar {
+  int *u;
+  int stride;
+  int i, j, c;
+
+  __device__ __forceinline__ int next_int() {
+    int iopt = u[(i - 1) * stride] - u[(j - 1) * stride];
+    if (iopt < 0) iopt += 16777216;
+    u[(i - 1) * stride] = iopt;
+    i -= 1;
+    j -= 1;
+    if (i == 0) i = 97;
+    else if (j == 0) j = 97;
+    c -= 7654321;
+    if (c < 0) c += 16777213;
+    iopt -= c;
+    if (iopt < 0) iopt += 16777216;
+    return iopt;
+  }
+};
+
+// Seed one stream exactly as initRandom (omc_random.c:75-123).
+__host__ __device__ inline void ranmar_seed(int ixx, int jxx, int *u, int stride) {
+  if (ixx <= 0 || ixx > 31328) ixx = 1802;
+  if (jxx <= 0 || jxx > 31328) jxx = 9373;
+  int i = (ixx / 177 % 177) + 2;
+  int j = (ixx % 177) + 2;
+  int k = (jxx / 169 % 178) + 1;
+  int l = (jxx % 169);
+  for (int ii = 0; ii < 97; ii++) {
+    int s = 0, t = 8388608;
+    for (int jj = 0; jj < 24; jj++) {
+      int m = ((i * j % 179) * k) % 179;
+      i = j;
+      j = k;
+      k = m;
+      l = (53 * l + 1) % 169;
+      if (l * m % 64 >= 32) s += t;
+      t /= 2;
+    }
+    u[ii * stride] = s;
+  }
+}
+
+// Seed pair of stream k: (ixx, jxx + k), continuing past 31328 into ixx + 1.
+__host__ __device__ inline void stream_seeds(int ixx, int jxx, long long k, int *ik, int *jk) {
+  if (ixx <= 0 || ixx > 31328) ixx = 1802;
+  if (jxx <= 0 || jxx > 31328) jxx = 9373;
+  long long lin = (long long)(jxx - 1) + k;
+  *jk = (int)(lin % 31328) + 1;
+  *ik = (int)(((long long)(ixx - 1) + lin / 31328) % 31328) + 1;
+}
+
+}  // namespace omcgpu

@@ -1,0 +1,599 @@
+// Transport engine: kernels, resident device state and the omc_engine_*
+// C ABI (include/omc_gpu.h).
+//
+// One run = nbatch launches of the persistent transport kernel, each
+// transporting nperbatch histories, each followed by the batch
+// accumulation (accumEndep, omc_dosxyz.c:696-717).  A lane (CUDA thread)
+// owns one RANMAR stream, seeded like the reference's OpenMP threads, and
+// one particle stack; lanes take histories from a global counter, the GPU
+// form of "#pragma omp parallel for schedule(dynamic)"
+// (omc_dosxyz.c:1252).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../host/common.h"
+#include "physics.cuh"
+
+using namespace omcgpu;
+using omc::fail;
+
+namespace {
+
+constexpr int kBlock = 128;  // lanes per block; the RNG state of a block is 97*kBlock ints of shared memory
+constexpr int kDefaultDepth = 48;
+
+#define CUDA_TRY(expr)                                                                           \
+  do {                                                                                           \
+    cudaError_t e_ = (expr);                                                                     \
+    if (e_ != cudaSuccess) return fail(OMC_ERR_CUDA, "%s: %s", #expr, cudaGetErrorString(e_)); \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// Kernels.
+// ---------------------------------------------------------------------------
+__global__ void seed_kernel(int ixx, int jxx, int nlanes, int *rng_u, int *rng_ijc) {
+  int lane = blockIdx.x * blockDim.x + threadIdx.x;
+  if (lane >= nlanes) return;
+  int ik, jk;
+  stream_seeds(ixx, jxx, lane, &ik, &jk);
+  ranmar_seed(ik, jk, rng_u + lane, nlanes);
+  rng_ijc[lane] = 97;
+  rng_ijc[nlanes + lane] = 33;
+  rng_ijc[2 * nlanes + lane] = 362436;
+}
+
+__global__ void ranmar_draw_kernel(int nlanes, long long n, int *rng_u, int *rng_ijc, int *out) {
+  int lane = blockIdx.x * blockDim.x + threadIdx.x;
+  if (lane >= nlanes) return;
+  Ranmar r;
+  r.u = rng_u + lane;
+  r.stride = nlanes;
+  r.i = rng_ijc[lane];
+  r.j = rng_ijc[nlanes + lane];
+  r.c = rng_ijc[2 * nlanes + lane];
+  for (long long k = 0; k < n; k++) out[static_cast<size_t>(lane) * n + k] = r.next_int();
+  rng_ijc[lane] = r.i;
+  rng_ijc[nlanes + lane] = r.j;
+  rng_ijc[2 * nlanes + lane] = r.c;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kBlock) transport_kernel(Params<R> P) {
+  extern __shared__ int s_rng[];  // [97][kBlock]
+  const int t = threadIdx.x;
+  const int lane = blockIdx.x * kBlock + t;
+  if (lane >= P.nlanes) return;
+  for (int k = 0; k < RNG_WORDS; k++) s_rng[k * kBlock + t] = P.rng_u[static_cast<size_t>(k) * P.nlanes + lane];
+  Lane<R> L(P, lane, s_rng + t, kBlock);
+  L.rng.i = P.rng_ijc[lane];
+  L.rng.j = P.rng_ijc[P.nlanes + lane];
+  L.rng.c = P.rng_ijc[2 * P.nlanes + lane];
+  unsigned long long events = 0;
+  long long hist_events = 0;
+  for (;;) {
+    if (L.np < 0) {
+      unsigned long long h = atomicAdd(P.next, 1ull);
+      if (h >= static_cast<unsigned long long>(P.nhist)) break;
+      L.init_history();
+      hist_events = 0;
+    }
+    if (L.p.iq == 0) L.photon_event();
+    else L.electron_event();
+    events++;
+    if (++hist_events > kEventCap) {
+      L.err |= ERR_EVENTS;
+      L.np = -1;
+    }
+  }
+  for (int k = 0; k < RNG_WORDS; k++) P.rng_u[static_cast<size_t>(k) * P.nlanes + lane] = s_rng[k * kBlock + t];
+  P.rng_ijc[lane] = L.rng.i;
+  P.rng_ijc[P.nlanes + lane] = L.rng.j;
+  P.rng_ijc[2 * P.nlanes + lane] = L.rng.c;
+  atomicAdd(P.ensrc, L.ensrc);
+  atomicAdd(P.events, events);
+  atomicMax(P.max_np, L.max_np);
+  if (L.err) atomicOr(P.err, L.err);
+}
+
+// Batch statistics: accum += e, accum2 += e^2, e = 0.
+__global__ void accumulate_kernel(double *endep, double *acc, double *acc2, long long n) {
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    double e = endep[i];
+    acc[i] += e;
+    acc2[i] += e * e;
+    endep[i] = 0.0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Device memory helpers.
+// ---------------------------------------------------------------------------
+struct DevBuf {
+  void *p = nullptr;
+  size_t n = 0;
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  omc_status ensure(size_t bytes) {
+    if (n >= bytes && p) return OMC_OK;
+    release();
+    if (cudaMalloc(&p, bytes) != cudaSuccess) {
+      p = nullptr;
+      return fail(OMC_ERR_NOMEM, "cudaMalloc of %zu bytes failed", bytes);
+    }
+    n = bytes;
+    return OMC_OK;
+  }
+};
+
+// A set of device arrays converted from host doubles to R.
+template <typename R>
+struct DevArrays {
+  std::vector<DevBuf> bufs;
+  void clear() {
+    for (auto &b : bufs) b.release();
+    bufs.clear();
+  }
+  const R *put(const double *src, size_t n) {
+    std::vector<R> h(n ? n : 1);
+    for (size_t i = 0; i < n; i++) h[i] = static_cast<R>(src[i]);
+    DevBuf b;
+    if (b.ensure(h.size() * sizeof(R)) != OMC_OK) return nullptr;
+    cudaMemcpy(b.p, h.data(), n * sizeof(R), cudaMemcpyHostToDevice);
+    bufs.push_back(b);
+    return static_cast<const R *>(b.p);
+  }
+  const int *put_int(const int *src, size_t n) {
+    DevBuf b;
+    if (b.ensure((n ? n : 1) * sizeof(int)) != OMC_OK) return nullptr;
+    cudaMemcpy(b.p, src, n * sizeof(int), cudaMemcpyHostToDevice);
+    bufs.push_back(b);
+    return static_cast<const int *>(b.p);
+  }
+};
+
+template <typename R>
+struct PrecisionState {
+  DevArrays<R> tables, geom, source;
+  Tables<R> T{};
+  Geometry<R> G{};
+  Source<R> S{};
+  DevBuf stk, key;
+  bool tables_ok = false, geom_ok = false, source_ok = false;
+};
+
+}  // namespace
+
+struct omc_engine {
+  int device = 0;
+  int nsm = 0;
+  cudaStream_t stream = nullptr;
+  PrecisionState<double> f64;
+  PrecisionState<float> f32;
+  // geometry scalars
+  int nreg = 0;
+  // per-lane RNG state
+  DevBuf rng_u, rng_ijc;
+  int seeded_lanes = 0, seeded_ixx = -1, seeded_jxx = -1;
+  // tallies and counters
+  DevBuf endep, acc, acc2, counters;
+  // host copies needed across uploads
+  omc_tables host_tables_dims{};
+};
+
+namespace {
+
+struct Counters {
+  unsigned long long next;
+  unsigned long long events;
+  double ensrc;
+  int max_np;
+  unsigned err;
+};
+
+template <typename R>
+omc_status upload_tables(PrecisionState<R> &S, const omc_tables *t) {
+  S.tables.clear();
+  int nmed = t->nmed;
+  size_t ng = static_cast<size_t>(nmed) * MXGE, ne = static_cast<size_t>(nmed) * MXEKE;
+  size_t nms = static_cast<size_t>(MXL_MS + 1) * (MXQ_MS + 1) * (MXU_MS + 1);
+  size_t nspin = static_cast<size_t>(nmed) * 2 * (MXE_SPIN1 + 1) * (MXQ_SPIN + 1) * (MXU_SPIN + 1);
+  DevArrays<R> &A = S.tables;
+  Tables<R> &T = S.T;
+  T.nmed = nmed;
+  T.ge0 = A.put(t->ge0, nmed);
+  T.ge1 = A.put(t->ge1, nmed);
+  T.eke0 = A.put(t->eke0, nmed);
+  T.eke1 = A.put(t->eke1, nmed);
+  T.xcc = A.put(t->xcc, nmed);
+  T.blcc = A.put(t->blcc, nmed);
+  T.te = A.put(t->te, nmed);
+  T.thmoll = A.put(t->thmoll, nmed);
+  T.ap = A.put(t->ap, nmed);
+  T.esig_e = A.put(t->esig_e, nmed);
+  T.psig_e = A.put(t->psig_e, nmed);
+  T.delcm = A.put(t->delcm, nmed);
+  T.zbrang = A.put(t->zbrang, nmed);
+  T.bpar0 = A.put(t->bpar0, nmed);
+  T.bpar1 = A.put(t->bpar1, nmed);
+  T.monotone = A.put_int(t->sig_ismonotone, 2 * nmed);
+  T.meke = A.put_int(t->meke, nmed);
+  T.gmfp0 = A.put(t->gmfp0, ng);
+  T.gmfp1 = A.put(t->gmfp1, ng);
+  T.gbr10 = A.put(t->gbr10, ng);
+  T.gbr11 = A.put(t->gbr11, ng);
+  T.gbr20 = A.put(t->gbr20, ng);
+  T.gbr21 = A.put(t->gbr21, ng);
+  T.cohe0 = A.put(t->cohe0, ng);
+  T.cohe1 = A.put(t->cohe1, ng);
+  T.pmax0 = A.put(t->pmax0, ng);
+  T.pmax1 = A.put(t->pmax1, ng);
+  // Rayleigh sampling reads medium 0's form-factor tables (see rayleigh()).
+  T.xgrid = A.put(t->xgrid, MXRAYFF);
+  T.fcum = A.put(t->fcum, MXRAYFF);
+  T.b_array = A.put(t->b_array, MXRAYFF);
+  T.c_array = A.put(t->c_array, MXRAYFF);
+  T.i_array = A.put_int(t->i_array, MXRAYFF);
+  T.dl1 = A.put(t->dl1, 8 * nmed);
+  T.dl2 = A.put(t->dl2, 8 * nmed);
+  T.dl3 = A.put(t->dl3, 8 * nmed);
+  T.dl4 = A.put(t->dl4, 8 * nmed);
+  T.dl5 = A.put(t->dl5, 8 * nmed);
+  T.dl6 = A.put(t->dl6, 8 * nmed);
+  T.esig0 = A.put(t->esig0, ne);
+  T.esig1 = A.put(t->esig1, ne);
+  T.psig0 = A.put(t->psig0, ne);
+  T.psig1 = A.put(t->psig1, ne);
+  T.ededx0 = A.put(t->ededx0, ne);
+  T.ededx1 = A.put(t->ededx1, ne);
+  T.pdedx0 = A.put(t->pdedx0, ne);
+  T.pdedx1 = A.put(t->pdedx1, ne);
+  T.ebr10 = A.put(t->ebr10, ne);
+  T.ebr11 = A.put(t->ebr11, ne);
+  T.pbr10 = A.put(t->pbr10, ne);
+  T.pbr11 = A.put(t->pbr11, ne);
+  T.pbr20 = A.put(t->pbr20, ne);
+  T.pbr21 = A.put(t->pbr21, ne);
+  T.tmxs0 = A.put(t->tmxs0, ne);
+  T.tmxs1 = A.put(t->tmxs1, ne);
+  T.blcce0 = A.put(t->blcce0, ne);
+  T.blcce1 = A.put(t->blcce1, ne);
+  T.etae0 = A.put(t->etae_ms0, ne);
+  T.etae1 = A.put(t->etae_ms1, ne);
+  T.etap0 = A.put(t->etap_ms0, ne);
+  T.etap1 = A.put(t->etap_ms1, ne);
+  T.q1ce0 = A.put(t->q1ce_ms0, ne);
+  T.q1ce1 = A.put(t->q1ce_ms1, ne);
+  T.q1cp0 = A.put(t->q1cp_ms0, ne);
+  T.q1cp1 = A.put(t->q1cp_ms1, ne);
+  T.q2ce0 = A.put(t->q2ce_ms0, ne);
+  T.q2ce1 = A.put(t->q2ce_ms1, ne);
+  T.q2cp0 = A.put(t->q2cp_ms0, ne);
+  T.q2cp1 = A.put(t->q2cp_ms1, ne);
+  T.e_array = A.put(t->e_array, ne);
+  T.range_ep = A.put(t->range_ep, 2 * ne);
+  T.b2spin_min = static_cast<R>(t->b2spin_min);
+  T.dbeta2i = static_cast<R>(t->dbeta2i);
+  T.espml = static_cast<R>(t->espml);
+  T.dleneri = static_cast<R>(t->dleneri);
+  T.dqq1i = static_cast<R>(t->dqq1i);
+  T.spin_rej = A.put(t->spin_rej, nspin);
+  T.ums = A.put(t->ums, nms);
+  T.fms = A.put(t->fms, nms);
+  T.wms = A.put(t->wms, nms);
+  T.ims = A.put_int(t->ims, nms);
+  T.dllambi = static_cast<R>(t->dllambi);
+  T.dqmsi = static_cast<R>(t->dqmsi);
+  for (auto &b : A.bufs)
+    if (!b.p) return fail(OMC_ERR_NOMEM, "table upload failed");
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(OMC_ERR_CUDA, "table upload: %s", cudaGetErrorString(e));
+  S.tables_ok = true;
+  return OMC_OK;
+}
+
+template <typename R>
+omc_status upload_geometry(PrecisionState<R> &S, const omc_phantom *ph, const std::vector<int8_t> &med,
+                           const std::vector<double> &rhof, const double *ecut_m, const double *pcut_m, int nmed) {
+  S.geom.clear();
+  DevArrays<R> &A = S.geom;
+  Geometry<R> &G = S.G;
+  G.nx = ph->nx;
+  G.ny = ph->ny;
+  G.nz = ph->nz;
+  G.nxy = ph->nx * ph->ny;
+  G.xb = A.put(ph->xbounds, ph->nx + 1);
+  G.yb = A.put(ph->ybounds, ph->ny + 1);
+  G.zb = A.put(ph->zbounds, ph->nz + 1);
+  G.rhof = A.put(rhof.data(), rhof.size());
+  G.ecut_m = A.put(ecut_m, nmed + 1);
+  G.pcut_m = A.put(pcut_m, nmed + 1);
+  DevBuf mb;
+  if (mb.ensure(med.size()) != OMC_OK) return OMC_ERR_NOMEM;
+  cudaMemcpy(mb.p, med.data(), med.size(), cudaMemcpyHostToDevice);
+  A.bufs.push_back(mb);
+  G.med = static_cast<const int8_t *>(mb.p);
+  for (auto &b : A.bufs)
+    if (!b.p) return fail(OMC_ERR_NOMEM, "geometry upload failed");
+  S.geom_ok = true;
+  return OMC_OK;
+}
+
+template <typename R>
+omc_status upload_source(PrecisionState<R> &S, const omc_source *s) {
+  S.source.clear();
+  Source<R> &D = S.S;
+  D.spectrum = s->spectrum;
+  D.charge = s->charge;
+  D.energy = static_cast<R>(s->energy);
+  D.deltak = static_cast<R>(s->deltak);
+  D.cdfinv1 = S.source.put(s->cdfinv1, OMC_INVDIM);
+  D.cdfinv2 = S.source.put(s->cdfinv2, OMC_INVDIM);
+  D.ssd = static_cast<R>(s->ssd);
+  D.xinl = static_cast<R>(s->xinl);
+  D.yinl = static_cast<R>(s->yinl);
+  D.xsize = static_cast<R>(s->xsize);
+  D.ysize = static_cast<R>(s->ysize);
+  D.ixinl = s->ixinl;
+  D.iyinl = s->iyinl;
+  if (!D.cdfinv1 || !D.cdfinv2) return fail(OMC_ERR_NOMEM, "source upload failed");
+  S.source_ok = true;
+  return OMC_OK;
+}
+
+template <typename R>
+omc_status run_batches(omc_engine *e, PrecisionState<R> &S, const omc_run_config *cfg, int nlanes, int depth,
+                       omc_run_stats *stats) {
+  size_t plane = static_cast<size_t>(depth) * nlanes;
+  if (S.stk.ensure(plane * 8 * sizeof(R)) != OMC_OK) return OMC_ERR_NOMEM;
+  if (S.key.ensure(plane * sizeof(int)) != OMC_OK) return OMC_ERR_NOMEM;
+  Counters *dc = static_cast<Counters *>(e->counters.p);
+  Params<R> P{};
+  P.T = S.T;
+  P.G = S.G;
+  P.S = S.S;
+  P.nsplit = cfg->nsplit < 1 ? 1 : cfg->nsplit;
+  P.nlanes = nlanes;
+  P.depth = depth;
+  P.nhist = cfg->nperbatch;
+  P.next = &dc->next;
+  P.rng_u = static_cast<int *>(e->rng_u.p);
+  P.rng_ijc = static_cast<int *>(e->rng_ijc.p);
+  P.stk = static_cast<R *>(S.stk.p);
+  P.stk_key = static_cast<int *>(S.key.p);
+  P.endep = static_cast<double *>(e->endep.p);
+  P.ensrc = &dc->ensrc;
+  P.events = &dc->events;
+  P.max_np = &dc->max_np;
+  P.err = &dc->err;
+  size_t smem = static_cast<size_t>(RNG_WORDS) * kBlock * sizeof(int);
+  cudaFuncSetAttribute(transport_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  int blocks = (nlanes + kBlock - 1) / kBlock;
+  cudaEvent_t t0, t1;
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  cudaEventRecord(t0, e->stream);
+  for (int b = 0; b < cfg->nbatch; b++) {
+    cudaMemsetAsync(&dc->next, 0, sizeof(unsigned long long), e->stream);
+    transport_kernel<R><<<blocks, kBlock, smem, e->stream>>>(P);
+    accumulate_kernel<<<std::max(1, std::min(4 * e->nsm, (e->nreg + 255) / 256)), 256, 0, e->stream>>>(
+        static_cast<double *>(e->endep.p), static_cast<double *>(e->acc.p), static_cast<double *>(e->acc2.p),
+        e->nreg);
+  }
+  cudaEventRecord(t1, e->stream);
+  cudaError_t err = cudaStreamSynchronize(e->stream);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, t0, t1);
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  if (err != cudaSuccess) return fail(OMC_ERR_CUDA, "transport: %s", cudaGetErrorString(err));
+  err = cudaGetLastError();
+  if (err != cudaSuccess) return fail(OMC_ERR_CUDA, "transport launch: %s", cudaGetErrorString(err));
+  Counters hc{};
+  cudaMemcpy(&hc, dc, sizeof hc, cudaMemcpyDeviceToHost);
+  if (stats) {
+    stats->ensrc = hc.ensrc;
+    stats->transport_ms = ms;
+    stats->histories = cfg->nperbatch * cfg->nbatch;
+    stats->steps = static_cast<long long>(hc.events);
+    stats->max_stack = hc.max_np + 1;
+    stats->error_flags = static_cast<int>(hc.err);
+  }
+  if (hc.err & ERR_STACK) return fail(OMC_ERR_STACK, "particle stack overflow (depth %d); histories were dropped", depth);
+  if (hc.err & (ERR_LOOP | ERR_EVENTS)) return fail(OMC_ERR_LIMIT, "a device loop hit its iteration limit");
+  return OMC_OK;
+}
+
+omc_status ensure_device(omc_engine *e) {
+  CUDA_TRY(cudaSetDevice(e->device));
+  return OMC_OK;
+}
+
+int default_lanes(omc_engine *e) {
+  int per_sm = 0;
+  size_t smem = static_cast<size_t>(RNG_WORDS) * kBlock * sizeof(int);
+  cudaFuncSetAttribute(transport_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, transport_kernel<float>, kBlock, smem);
+  if (per_sm < 1) per_sm = 1;
+  return e->nsm * per_sm * kBlock;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" omc_status omc_engine_create(int device, omc_engine **out) {
+  if (!out) return fail(OMC_ERR_ARG, "null argument");
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return fail(OMC_ERR_CUDA, "no CUDA device available");
+  if (device < 0 || device >= n) return fail(OMC_ERR_ARG, "device %d outside 0..%d", device, n - 1);
+  auto *e = new omc_engine();
+  e->device = device;
+  if (cudaSetDevice(device) != cudaSuccess) {
+    delete e;
+    return fail(OMC_ERR_CUDA, "cudaSetDevice(%d) failed", device);
+  }
+  cudaDeviceGetAttribute(&e->nsm, cudaDevAttrMultiProcessorCount, device);
+  cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
+  if (e->counters.ensure(sizeof(Counters)) != OMC_OK) {
+    delete e;
+    return OMC_ERR_NOMEM;
+  }
+  *out = e;
+  return OMC_OK;
+}
+
+extern "C" void omc_engine_destroy(omc_engine *e) {
+  if (!e) return;
+  cudaSetDevice(e->device);
+  cudaStreamSynchronize(e->stream);
+  e->f64.tables.clear();
+  e->f64.geom.clear();
+  e->f64.source.clear();
+  e->f64.stk.release();
+  e->f64.key.release();
+  e->f32.tables.clear();
+  e->f32.geom.clear();
+  e->f32.source.clear();
+  e->f32.stk.release();
+  e->f32.key.release();
+  e->rng_u.release();
+  e->rng_ijc.release();
+  e->endep.release();
+  e->acc.release();
+  e->acc2.release();
+  e->counters.release();
+  cudaStreamDestroy(e->stream);
+  delete e;
+}
+
+extern "C" omc_status omc_engine_set_tables(omc_engine *e, const omc_tables *t) {
+  if (!e || !t) return fail(OMC_ERR_ARG, "null argument");
+  omc_status s;
+  if ((s = ensure_device(e)) != OMC_OK) return s;
+  if ((s = upload_tables(e->f64, t)) != OMC_OK) return s;
+  if ((s = upload_tables(e->f32, t)) != OMC_OK) return s;
+  e->host_tables_dims.nmed = t->nmed;
+  return OMC_OK;
+}
+
+extern "C" omc_status omc_engine_set_geometry(omc_engine *e, const omc_phantom *ph, const omc_regions *r) {
+  if (!e || !ph || !r) return fail(OMC_ERR_ARG, "null argument");
+  if (!e->f64.tables_ok) return fail(OMC_ERR_STATE, "omc_engine_set_tables must come first");
+  int nmed = e->host_tables_dims.nmed;
+  int nreg = ph->nx * ph->ny * ph->nz + 1;
+  if (r->nreg != nreg) return fail(OMC_ERR_ARG, "regions (%d) do not match the phantom (%d)", r->nreg, nreg);
+  std::vector<int8_t> med(nreg);
+  std::vector<double> rhof(r->rhof, r->rhof + nreg);
+  // ecut/pcut are per region in the reference; initRegions makes them a
+  // function of the medium, which is what the device stores.
+  std::vector<double> ecut_m(nmed + 1, 0.0), pcut_m(nmed + 1, 0.0);
+  std::vector<int> seen(nmed + 1, 0);
+  for (int i = 0; i < nreg; i++) {
+    int m = r->med[i];
+    if (m < -1 || m >= nmed) return fail(OMC_ERR_ARG, "region %d: medium %d outside -1..%d", i, m, nmed - 1);
+    med[i] = static_cast<int8_t>(m);
+    if (i == 0) continue;
+    if (!seen[m + 1]) {
+      ecut_m[m + 1] = r->ecut[i];
+      pcut_m[m + 1] = r->pcut[i];
+      seen[m + 1] = 1;
+    } else if (ecut_m[m + 1] != r->ecut[i] || pcut_m[m + 1] != r->pcut[i]) {
+      return fail(OMC_ERR_ARG, "region %d: ecut/pcut differ within medium %d", i, m);
+    }
+  }
+  ecut_m[0] = 0.0;
+  pcut_m[0] = 0.0;
+  omc_status s;
+  if ((s = ensure_device(e)) != OMC_OK) return s;
+  if ((s = upload_geometry(e->f64, ph, med, rhof, ecut_m.data(), pcut_m.data(), nmed)) != OMC_OK) return s;
+  if ((s = upload_geometry(e->f32, ph, med, rhof, ecut_m.data(), pcut_m.data(), nmed)) != OMC_OK) return s;
+  e->nreg = nreg;
+  if ((s = e->endep.ensure(nreg * sizeof(double))) != OMC_OK) return s;
+  if ((s = e->acc.ensure(nreg * sizeof(double))) != OMC_OK) return s;
+  if ((s = e->acc2.ensure(nreg * sizeof(double))) != OMC_OK) return s;
+  return OMC_OK;
+}
+
+extern "C" omc_status omc_engine_set_source(omc_engine *e, const omc_source *s) {
+  if (!e || !s) return fail(OMC_ERR_ARG, "null argument");
+  omc_status st;
+  if ((st = ensure_device(e)) != OMC_OK) return st;
+  if ((st = upload_source(e->f64, s)) != OMC_OK) return st;
+  if ((st = upload_source(e->f32, s)) != OMC_OK) return st;
+  return OMC_OK;
+}
+
+static omc_status engine_run(omc_engine *e, const omc_run_config *cfg, omc_run_stats *stats) {
+  if (!e || !cfg) return fail(OMC_ERR_ARG, "null argument");
+  if (!e->f64.tables_ok || !e->f64.geom_ok || !e->f64.source_ok)
+    return fail(OMC_ERR_STATE, "tables, geometry and source must be set before a run");
+  if (cfg->nbatch < 1 || cfg->nperbatch < 0) return fail(OMC_ERR_ARG, "nbatch must be >= 1 and nperbatch >= 0");
+  if (cfg->precision != OMC_FP64 && cfg->precision != OMC_FP32) return fail(OMC_ERR_ARG, "unknown precision");
+  omc_status s;
+  if ((s = ensure_device(e)) != OMC_OK) return s;
+  int nlanes = cfg->serial ? 1 : (cfg->nlanes > 0 ? cfg->nlanes : default_lanes(e));
+  int depth = cfg->stack_depth > 0 ? cfg->stack_depth : kDefaultDepth + 4 * std::max(1, cfg->nsplit);
+  // RANMAR streams, one per lane, seeded for this run.
+  if ((s = e->rng_u.ensure(static_cast<size_t>(RNG_WORDS) * nlanes * sizeof(int))) != OMC_OK) return s;
+  if ((s = e->rng_ijc.ensure(static_cast<size_t>(3) * nlanes * sizeof(int))) != OMC_OK) return s;
+  seed_kernel<<<(nlanes + 255) / 256, 256, 0, e->stream>>>(cfg->ixx, cfg->jxx, nlanes, static_cast<int *>(e->rng_u.p),
+                                                          static_cast<int *>(e->rng_ijc.p));
+  cudaMemsetAsync(e->endep.p, 0, e->nreg * sizeof(double), e->stream);
+  cudaMemsetAsync(e->acc.p, 0, e->nreg * sizeof(double), e->stream);
+  cudaMemsetAsync(e->acc2.p, 0, e->nreg * sizeof(double), e->stream);
+  cudaMemsetAsync(e->counters.p, 0, sizeof(Counters), e->stream);
+  if (cfg->precision == OMC_FP64) return run_batches(e, e->f64, cfg, nlanes, depth, stats);
+  return run_batches(e, e->f32, cfg, nlanes, depth, stats);
+}
+
+extern "C" omc_status omc_engine_run(omc_engine *e, const omc_run_config *cfg, double *accum_endep,
+                                     double *accum_endep2, omc_run_stats *stats) {
+  omc_status s = engine_run(e, cfg, stats);
+  if (s != OMC_OK && s != OMC_ERR_STACK && s != OMC_ERR_LIMIT) return s;
+  if (accum_endep) cudaMemcpy(accum_endep, e->acc.p, e->nreg * sizeof(double), cudaMemcpyDeviceToHost);
+  if (accum_endep2) cudaMemcpy(accum_endep2, e->acc2.p, e->nreg * sizeof(double), cudaMemcpyDeviceToHost);
+  return s;
+}
+
+extern "C" omc_status omc_engine_run_resident(omc_engine *e, const omc_run_config *cfg, const double **d_acc,
+                                              const double **d_acc2, omc_run_stats *stats) {
+  omc_status s = engine_run(e, cfg, stats);
+  if (d_acc) *d_acc = static_cast<const double *>(e->acc.p);
+  if (d_acc2) *d_acc2 = static_cast<const double *>(e->acc2.p);
+  return s;
+}
+
+extern "C" void omc_stream_seeds(int ixx, int jxx, long long k, int *ixx_k, int *jxx_k) {
+  stream_seeds(ixx, jxx, k, ixx_k, jxx_k);
+}
+
+extern "C" omc_status omc_gpu_ranmar(int device, int ixx, int jxx, int nstreams, long long n, int32_t *out) {
+  if (!out || nstreams < 1 || n < 0) return fail(OMC_ERR_ARG, "bad argument");
+  CUDA_TRY(cudaSetDevice(device));
+  DevBuf u, ijc, o;
+  omc_status s;
+  if ((s = u.ensure(static_cast<size_t>(RNG_WORDS) * nstreams * sizeof(int))) != OMC_OK) return s;
+  if ((s = ijc.ensure(static_cast<size_t>(3) * nstreams * sizeof(int))) != OMC_OK) return s;
+  if ((s = o.ensure(static_cast<size_t>(nstreams) * (n ? n : 1) * sizeof(int))) != OMC_OK) return s;
+  seed_kernel<<<(nstreams + 255) / 256, 256>>>(ixx, jxx, nstreams, static_cast<int *>(u.p), static_cast<int *>(ijc.p));
+  ranmar_draw_kernel<<<(nstreams + 127) / 128, 128>>>(nstreams, n, static_cast<int *>(u.p), static_cast<int *>(ijc.p),
+                                                     static_cast<int *>(o.p));
+  cudaError_t err = cudaDeviceSynchronize();
+  if (err == cudaSuccess)
+    err = cudaMemcpy(out, o.p, static_cast<size_t>(nstreams) * n * sizeof(int), cudaMemcpyDeviceToHost);
+  u.release();
+  ijc.release();
+  o.release();
+  if (err != cudaSuccess) return fail(OMC_ERR_CUDA, "ranmar: %s", cudaGetErrorString(err));
+  return OMC_OK;
+}

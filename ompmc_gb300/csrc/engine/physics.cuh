@@ -1,0 +1,327 @@
+// Photon/electron transport physics of one lane (one CUDA thread).
+//
+// Each routine restates the reference routine named in its comment
+// (edoerner/ompMC src/ompmc.c, ucodes/omc_dosxyz/omc_dosxyz.c) with the same
+// random-number consumption, so a lane processes its histories exactly as a
+// thread of the reference does; R is the transport precision (double or
+// float), tallies are always FP64.
+//
+// Stack discipline: the top particle lives in registers (p, at slot np);
+// slots 0..np-1 live in HBM in the lane's interleaved stack.
+#pragma once
+
+#include "device.cuh"
+
+namespace omcgpu {
+
+#define RC(x) static_cast<R>(x)
+
+template <typename R>
+__device__ __forceinline__ R pwlf(const R *c1, const R *c0, int idx, R lv) {
+  return lv * __ldg(c1 + idx) + __ldg(c0 + idx);
+}
+
+template <typename R>
+struct Lane {
+  const Params<R> &P;
+  Ranmar rng;
+  int lane;
+  int np;  // top slot, -1 = empty
+  Particle<R> p;
+  double ensrc;
+  unsigned err;
+  int max_np;
+
+  __device__ Lane(const Params<R> &prm, int ln, int *su, int sstride) : P(prm), lane(ln) {
+    rng.u = su;
+    rng.stride = sstride;
+    np = -1;
+    ensrc = 0.0;
+    err = 0;
+    max_np = 0;
+  }
+
+  __device__ __forceinline__ R rnd() { return static_cast<R>(rng.next_int()) * RC(1.0 / 16777216.0); }
+
+  // ---- stack --------------------------------------------------------------
+  __device__ __forceinline__ size_t sidx(int slot) const {
+    return static_cast<size_t>(slot) * P.nlanes + lane;
+  }
+  __device__ __forceinline__ void store(int slot, const Particle<R> &q) {
+    size_t i = sidx(slot), plane = static_cast<size_t>(P.depth) * P.nlanes;
+    R *s = P.stk;
+    s[i] = q.e;
+    s[i + plane] = q.x;
+    s[i + 2 * plane] = q.y;
+    s[i + 3 * plane] = q.z;
+    s[i + 4 * plane] = q.u;
+    s[i + 5 * plane] = q.v;
+    s[i + 6 * plane] = q.w;
+    s[i + 7 * plane] = q.wt;
+    P.stk_key[i] = q.ir * 4 + (q.iq + 1);
+  }
+  __device__ __forceinline__ void load(int slot, Particle<R> &q) const {
+    size_t i = sidx(slot), plane = static_cast<size_t>(P.depth) * P.nlanes;
+    const R *s = P.stk;
+    q.e = s[i];
+    q.x = s[i + plane];
+    q.y = s[i + 2 * plane];
+    q.z = s[i + 3 * plane];
+    q.u = s[i + 4 * plane];
+    q.v = s[i + 5 * plane];
+    q.w = s[i + 6 * plane];
+    q.wt = s[i + 7 * plane];
+    int key = P.stk_key[i];
+    q.ir = key >> 2;
+    q.iq = (key & 3) - 1;
+  }
+  // The top (p) goes to memory and q becomes the new top.  False (history
+  // dropped, error flagged) if the lane's stack is full.
+  __device__ __forceinline__ bool push(const Particle<R> &q) {
+    if (np + 1 >= P.depth) {
+      err |= ERR_STACK;
+      np = -1;
+      return false;
+    }
+    store(np, p);
+    np += 1;
+    p = q;
+    if (np > max_np) max_np = np;
+    return true;
+  }
+  __device__ __forceinline__ void pop() {
+    np -= 1;
+    if (np >= 0) load(np, p);
+  }
+
+  // ---- scoring: ausgab (omc_dosxyz.c:683-694) ------------------------------
+  __device__ __forceinline__ void ausgab(int ir, R wt, R edep) {
+    atomicAdd(P.endep + ir, static_cast<double>(wt * edep));
+  }
+
+  // ---- geometry: region decode, howfar, hownear (omc_dosxyz.c:187-334) ----
+  __device__ __forceinline__ int med_of(int ir) const { return P.G.med[ir]; }
+  __device__ __forceinline__ R rhof_of(int ir) const { return __ldg(P.G.rhof + ir); }
+  __device__ __forceinline__ R ecut_of(int ir) const { return __ldg(P.G.ecut_m + P.G.med[ir] + 1); }
+  __device__ __forceinline__ R pcut_of(int ir) const { return __ldg(P.G.pcut_m + P.G.med[ir] + 1); }
+
+  __device__ void howfar(const Particle<R> &q, int &idisc, int &irnew, R &ustep) const {
+    const Geometry<R> &g = P.G;
+    int irl = q.ir;
+    if (irl == 0) {
+      idisc = 1;
+      return;
+    }
+    int irx = (irl - 1) % g.nx;
+    int irz = (irl - 1 - irx) / g.nxy;
+    int iry = ((irl - 1 - irx) - irz * g.nxy) / g.nx;
+    R dist;
+    if (q.w > RC(0)) {
+      dist = (__ldg(g.zb + irz + 1) - q.z) / q.w;
+      if (dist < ustep) {
+        ustep = dist;
+        irnew = (irz != g.nz - 1) ? irl + g.nxy : 0;
+      }
+    } else if (q.w < RC(0)) {
+      dist = -(q.z - __ldg(g.zb + irz)) / q.w;
+      if (dist < ustep) {
+        ustep = dist;
+        irnew = (irz != 0) ? irl - g.nxy : 0;
+      }
+    }
+    if (q.u > RC(0)) {
+      dist = (__ldg(g.xb + irx + 1) - q.x) / q.u;
+      if (dist < ustep) {
+        ustep = dist;
+        irnew = (irx != g.nx - 1) ? irl + 1 : 0;
+      }
+    } else if (q.u < RC(0)) {
+      dist = -(q.x - __ldg(g.xb + irx)) / q.u;
+      if (dist < ustep) {
+        ustep = dist;
+        irnew = (irx != 0) ? irl - 1 : 0;
+      }
+    }
+    if (q.v > RC(0)) {
+      dist = (__ldg(g.yb + iry + 1) - q.y) / q.v;
+      if (dist < ustep) {
+        ustep = dist;
+        irnew = (iry != g.ny - 1) ? irl + g.nx : 0;
+      }
+    } else if (q.v < RC(0)) {
+      dist = -(q.y - __ldg(g.yb + iry)) / q.v;
+      if (dist < ustep) {
+        ustep = dist;
+        irnew = (iry != 0) ? irl - g.nx : 0;
+      }
+    }
+  }
+
+  __device__ R hownear(const Particle<R> &q) const {
+    const Geometry<R> &g = P.G;
+    int irl = q.ir;
+    if (irl == 0) return RC(0);
+    int irx = (irl - 1) % g.nx;
+    int irz = (irl - 1 - irx) / g.nxy;
+    int iry = ((irl - 1 - irx) - irz * g.nxy) / g.nx;
+    R t = RC(1.0E10);
+    t = fmin(t, __ldg(g.xb + irx + 1) - q.x);
+    t = fmin(t, q.x - __ldg(g.xb + irx));
+    t = fmin(t, __ldg(g.yb + iry + 1) - q.y);
+    t = fmin(t, q.y - __ldg(g.yb + iry));
+    t = fmin(t, __ldg(g.zb + irz + 1) - q.z);
+    t = fmin(t, q.z - __ldg(g.zb + irz));
+    return t;
+  }
+
+  // ---- interpolation indices, clamped to the table --------------------------
+  __device__ __forceinline__ int photon_bin(int imed, R gle) {
+    int l = static_cast<int>(gle * __ldg(P.T.ge1 + imed) + __ldg(P.T.ge0 + imed)) - 1;
+    if (l < 0 || l >= MXGE) {
+      err |= ERR_TABLE;
+      l = l < 0 ? 0 : MXGE - 1;
+    }
+    return l;
+  }
+  __device__ __forceinline__ int electron_bin(int imed, R elke) {
+    int l = static_cast<int>(elke * __ldg(P.T.eke1 + imed) + __ldg(P.T.eke0 + imed)) - 1;
+    int top = __ldg(P.T.meke + imed) - 1;
+    if (l < 0 || l > top) {
+      err |= ERR_TABLE;
+      l = l < 0 ? 0 : top;
+    }
+    return l;
+  }
+
+  // ---- rotations (ompmc.c:101-201) ------------------------------------------
+  struct Uphi {
+    R A, B, C, cosphi, sinphi;
+  };
+
+  __device__ void azimuth(R &cphi, R &sphi) {
+    R xphi, xphi2, yphi, yphi2, rhophi2;
+    int guard = 0;
+    do {
+      xphi = rnd();
+      xphi = RC(2) * xphi - RC(1);
+      xphi2 = xphi * xphi;
+      yphi = rnd();
+      yphi2 = yphi * yphi;
+      rhophi2 = xphi2 + yphi2;
+      if (++guard > kRejectCap) {
+        err |= ERR_LOOP;
+        break;
+      }
+    } while (rhophi2 > RC(1));
+    rhophi2 = RC(1) / rhophi2;
+    cphi = (xphi2 - yphi2) * rhophi2;
+    sphi = RC(2) * xphi * yphi * rhophi2;
+  }
+
+  __device__ __forceinline__ static void rotate(Particle<R> &q, const Uphi &up, R costhe, R sinthe) {
+    R sinps2 = up.A * up.A + up.B * up.B;
+    if (sinps2 < RC(1.0E-20)) {
+      q.u = sinthe * up.cosphi;
+      q.v = sinthe * up.sinphi;
+      q.w = up.C * costhe;
+    } else {
+      R sinpsi = sqrt(sinps2);
+      R us = sinthe * up.cosphi;
+      R vs = sinthe * up.sinphi;
+      R sindel = up.B / sinpsi;
+      R cosdel = up.A / sinpsi;
+      q.u = up.C * cosdel * us - sindel * vs + up.A * costhe;
+      q.v = up.C * sindel * us + cosdel * vs + up.B * costhe;
+      q.w = -sinpsi * us + up.C * costhe;
+    }
+  }
+
+  // uphi21: new direction of q itself, azimuth sampled here.
+  __device__ void uphi21(Particle<R> &q, Uphi &up, R costhe, R sinthe) {
+    azimuth(up.cosphi, up.sinphi);
+    up.A = q.u;
+    up.B = q.v;
+    up.C = q.w;
+    rotate(q, up, costhe, sinthe);
+  }
+  // uphi32: a second particle at the position of `from`, rotated from the
+  // direction saved in up (transferProperties + rotation, ompmc.c:166-201).
+  __device__ static void uphi32(Particle<R> &q, const Particle<R> &from, const Uphi &up, R costhe, R sinthe) {
+    q.x = from.x;
+    q.y = from.y;
+    q.z = from.z;
+    q.ir = from.ir;
+    q.wt = from.wt;
+    rotate(q, up, costhe, sinthe);
+  }
+
+#include "photon.inc"
+#include "electron.inc"
+
+  // ---- source: initHistory (omc_dosxyz.c:964-1068) --------------------------
+  __device__ void init_history() {
+    const Source<R> &s = P.S;
+    const Geometry<R> &g = P.G;
+    Particle<R> q;
+    q.iq = s.charge;
+    R ein;
+    if (s.spectrum) {
+      R rnno1 = rnd();
+      R rnno2 = rnd();
+      int k = static_cast<int>(fmin(s.deltak * rnno1, s.deltak - RC(1)));
+      ein = __ldg(s.cdfinv1 + k) + rnno2 * __ldg(s.cdfinv2 + k);
+    } else {
+      ein = s.energy;
+    }
+    q.e = (q.iq != 0) ? ein + RC(0.5109989461) : ein;
+    ensrc += static_cast<double>(ein);
+    R rxyz;
+    if (s.xsize == RC(0) || s.ysize == RC(0)) {
+      q.x = s.xinl;
+      q.y = s.yinl;
+      rxyz = sqrt(s.ssd * s.ssd + q.x * q.x + q.y * q.y);
+      q.w = s.ssd / rxyz;
+    } else {
+      R fw, rnno3;
+      int guard = 0;
+      do {
+        rnno3 = rnd();
+        q.x = rnno3 * s.xsize + s.xinl;
+        rnno3 = rnd();
+        q.y = rnno3 * s.ysize + s.yinl;
+        rnno3 = rnd();
+        rxyz = sqrt(s.ssd * s.ssd + q.x * q.x + q.y * q.y);
+        q.w = s.ssd / rxyz;
+        fw = q.w * q.w * q.w;
+        if (++guard > kRejectCap) {
+          err |= ERR_LOOP;
+          break;
+        }
+      } while (rnno3 >= fw);
+    }
+    q.z = __ldg(g.zb + 0);
+    q.u = q.x / rxyz;
+    q.v = q.y / rxyz;
+    int ix, iy;
+    if (s.xsize == RC(0)) {
+      ix = s.ixinl;
+    } else {
+      ix = s.ixinl - 1;
+      while ((__ldg(g.xb + ix + 1) < q.x) && ix < g.nx - 1) ix++;
+    }
+    if (s.ysize == RC(0)) {
+      iy = s.iyinl;
+    } else {
+      iy = s.iyinl - 1;
+      while ((__ldg(g.yb + iy + 1) < q.y) && iy < g.ny - 1) iy++;
+    }
+    q.ir = 1 + ix + iy * g.nx;
+    q.wt = RC(1);
+    p = q;
+    np = 0;
+  }
+};
+
+#undef RC
+
+}  // namespace omcgpu

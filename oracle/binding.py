@@ -11,12 +11,13 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import platform
 import subprocess
 
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB = os.path.join(HERE, "liboracle.so")
+LIB = os.path.join(HERE, "_build", platform.machine(), "liboracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
 
 
@@ -29,7 +30,7 @@ _lib = None
 
 
 def build():
-    subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
+    subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True, capture_output=True)
 
 
 def lib():
