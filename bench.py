@@ -1,0 +1,352 @@
+"""Benchmark of the GB300 transport on the 6 MV heterogeneous slab.
+
+Workload (one "step" = one statistical batch of HISTORIES_PER_STEP
+histories): the 150^3 slab phantom at 2 mm voxels (water 0-5 cm, lung
+0.26 g/cm^3 5-15 cm, ICRP bone 1.85 g/cm^3 15-18 cm, water 18-30 cm), the
+synthetic 24-bin 6 MV spectrum, a 10x10 cm^2 field from a point source at
+SSD 100 cm, ECUT 0.700 / PCUT 0.010 MeV, 700icru media.  Ten steps are the
+1e8-history job of that configuration.
+
+Prints one JSON line: FP32-transport (FP64 tallies) histories/s as
+`value`, the plain FP64 path beside it, the statistical efficiency
+1/(s^2 T), the end-to-end rate through the C ABI with host buffers, the
+roofline of the transport kernel, the CPU baseline (the oracle port on all
+host cores) and the SM clocks seen during the timed region.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "6MV heterogeneous slab 150^3 @ 2 mm, 10x10 cm2 field, SSD 100 cm"
+HISTORIES_PER_STEP = 10_000_000
+FP64_HISTORIES = 1_000_000
+LANES_PER_RANK_STRIDE = 1 << 21  # stream-index stride between ranks (> lanes of one GPU)
+L2_FLUSH_BYTES = 256 << 20       # larger than the 129 MB L2
+
+
+def build_problem(tmp):
+    from ompmc_gb300 import api, data
+    from ompmc_gb300 import workloads as W
+
+    data.stage()
+    P = data.paths()
+    ph = W.slab(n=150, vox=0.2)
+    phantom = api.Phantom.from_arrays(ph.media, ph.xb, ph.yb, ph.zb, ph.med, ph.rho)
+    spec = W.write_spectrum(os.path.join(tmp, "6mv.spectrum"), "synthetic 6 MV", *W.spectrum_6mv())
+    job = W.Job("(in memory)", P["pegs"], P["pgs4form"], P["data_folder"], tmp + os.sep, spectrum_file=spec,
+                ncase=10 * HISTORIES_PER_STEP, nbatch=10, collimator=(-5.0, 5.0, -5.0, 5.0), ssd=100.0)
+    return api.Problem(api.Input(text=job.text()), phantom=phantom)
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,utilization.gpu,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 10:
+                continue
+            try:
+                util = float(f[4])
+                if util < 50:
+                    continue
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[6:10]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per history of the transport kernel from the committed
+    ncu summary (profiles/), or None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "transport_fp32_slab150.json")) as f:
+            return float(json.load(f)["dram_bytes_per_history"])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def max_rel_sigma(acc, acc2, nb, frac=0.5):
+    """max over voxels with dose > frac*Dmax of the batch relative
+    uncertainty (accumulateResults, omc_dosxyz.c:739-751)."""
+    m = acc[1:] / nb
+    m2 = acc2[1:] / nb
+    sel = m > frac * m.max()
+    s = np.sqrt(np.maximum(m2[sel] - m[sel] ** 2, 0.0) / (nb - 1)) / m[sel]
+    return float(s.max())
+
+
+def cpu_oracle_sample(prob, target_seconds=8.0, cap=5_000_000):
+    """The oracle port on every host core, on a sample of the workload sized
+    to about target_seconds of wall time."""
+    from oracle import binding as oracle
+
+    oracle.build()
+    probe = 20000
+    _, _, r = oracle.run(prob, nperbatch=probe // 2, nbatch=2, nthreads=0)
+    rate = probe / max(r.seconds, 1e-6)
+    n = int(min(cap, max(probe, rate * target_seconds)))
+    n -= n % 2
+    _, _, r = oracle.run(prob, nperbatch=n // 2, nbatch=2, nthreads=0)
+    return n / r.seconds, r.nthreads, n, r.seconds
+
+
+def run_reference_arm(args, rank):
+    if rank != 0:
+        return
+    with tempfile.TemporaryDirectory() as tmp:
+        prob = build_problem(tmp)
+        rates, cores, n = [], 0, 0
+        for step in range(args.warmup + args.steps):
+            rate, cores, n, secs = cpu_oracle_sample(prob, target_seconds=4.0)
+            if step >= args.warmup:
+                rates.append((n, secs))
+        tot_n = sum(r[0] for r in rates)
+        tot_s = sum(r[1] for r in rates)
+        value = tot_n / tot_s
+        line = {
+            "impl": "reference", "metric": "histories/s", "value": value, "unit": "histories/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * tot_s / len(rates), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "histories_per_step": n,
+                       "note": "reference CPU path = oracle port (C restatement, OpenMP, dynamic schedule); "
+                               "the reference's own x86 build cannot run on the aarch64 host"},
+            "cpu_baseline": {"value": value, "unit": "histories/s", "cores": cores, "kind": "port",
+                             "sample": f"{n} histories per step of the workload"},
+            "e2e": {"value": value, "unit": "histories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, local_rank, dist_on):
+    import torch
+
+    from ompmc_gb300 import api
+    from ompmc_gb300 import dist as D
+
+    torch.cuda.set_device(local_rank)
+    flush_buf = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local_rank}")
+
+    def flush_l2():
+        flush_buf.zero_()
+        torch.cuda.synchronize()
+
+    def barrier():
+        if dist_on:
+            import torch.distributed as tdist
+
+            tdist.barrier()
+        torch.cuda.synchronize()
+
+    with tempfile.TemporaryDirectory() as tmp:
+        prob = build_problem(tmp)
+        eng = api.Engine(local_rank).load(prob)
+        seeds = D.rank_seeds(97, 33, rank, LANES_PER_RANK_STRIDE)
+        H = args.histories_per_step
+        cfg32 = api.Engine.config(H, 1, seeds=seeds, precision=api.FP32)
+        # warm-up
+        for _ in range(args.warmup):
+            flush_l2()
+            eng.run_resident(cfg32)  # seeds the streams the timed batches continue
+        # timed region: K batches of H histories, FP32 transport / FP64 tallies
+        sampler = ClockSampler(local_rank)
+        barrier()
+        sampler.start()
+        step_ms, geo, dep, evs = [], 0, 0, 0
+        acc = np.zeros(prob.nreg)
+        acc2 = np.zeros(prob.nreg)
+        launches = 0
+        for k in range(args.steps):
+            flush_l2()
+            # successive batches of one job: the streams continue
+            a, _, st = eng.run(nperbatch=H, nbatch=1, seeds=seeds, precision=api.FP32, continue_streams=1)
+            if st.error_flags:
+                raise RuntimeError(f"device error flags {st.error_flags:#x}")
+            step_ms.append(st.kernel_ms)
+            geo += st.voxel_steps
+            dep += st.deposits
+            evs += st.steps
+            acc += a
+            acc2 += a * a
+            launches += 2  # transport, batch accumulation (streams continue: no seeding)
+        barrier()
+        clocks = sampler.stop()
+        dev_ms = float(sum(step_ms))
+        if dist_on:
+            import torch.distributed as tdist
+
+            t = torch.tensor([dev_ms], dtype=torch.float64, device=f"cuda:{local_rank}")
+            tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+            dev_ms = float(t.item())
+        total_hist = world * args.steps * H
+        value = total_hist / (dev_ms / 1000.0)
+        s = max_rel_sigma(acc, acc2, args.steps) if args.steps >= 2 else None
+        efficiency = 1.0 / (s * s * dev_ms / 1000.0) if s else None
+        # plain FP64 path, same workload, fewer histories
+        cfg64 = api.Engine.config(FP64_HISTORIES, 1, seeds=seeds, precision=api.FP64)
+        eng.run_resident(cfg64)
+        f64 = []
+        for _ in range(2):
+            flush_l2()
+            _, _, st = eng.run_resident(cfg64)
+            f64.append(st.kernel_ms)
+        fp64_value = FP64_HISTORIES / (statistics.mean(f64) / 1000.0)
+        # end to end through the C ABI: phantom upload, transport, tallies back
+        e2e_steps = max(1, min(args.steps, 3))
+        ph = prob.phantom
+        regs = prob.regions
+        h2d = prob.nreg * (1 + 4 + 8) + 8 * (sum(ph.shape) + 3) * 2
+        d2h = 2 * prob.nreg * 8
+        barrier()
+        t0 = time.perf_counter()
+        for k in range(e2e_steps):
+            eng.set_geometry(prob)
+            a, a2, st = eng.run(nperbatch=H, nbatch=1, seeds=seeds, precision=api.FP32)
+        torch.cuda.synchronize()
+        e2e_s = time.perf_counter() - t0
+        e2e_value = world * e2e_steps * H / e2e_s
+        # roofline of the transport kernel
+        peak, peak_kind = measured_peaks()
+        per_hist_bytes = (8.0 * geo + 8.0 * dep) / (args.steps * H) + 16.0
+        launch_s = dev_ms / 1000.0 / args.steps
+        achieved = per_hist_bytes * H / launch_s / 1e9
+        traffic_ph = profiled_traffic()
+        line = None
+        if rank == 0:
+            cpu = None
+            if world == 1 and not args.no_cpu_baseline:
+                rate, cores, n, secs = cpu_oracle_sample(prob)
+                cpu = {"value": rate, "unit": "histories/s", "cores": cores, "kind": "port",
+                       "sample": f"{n} histories of the workload (oracle port, OpenMP dynamic schedule), {secs:.1f} s"}
+            lat = sorted(step_ms)
+            line = {
+                "metric": "histories/s", "value": value, "unit": "histories/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic",
+                "config": {"workload": WORKLOAD, "histories_per_step": H, "global_histories": total_hist,
+                           "transport": "FP32 arithmetic, FP64 tallies and energy balance",
+                           "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{world}"},
+                "fp64": {"value": fp64_value, "unit": "histories/s", "histories_per_step": FP64_HISTORIES},
+                "fp32_over_fp64": value / world / fp64_value,
+                "efficiency": {"value": efficiency, "unit": "1/(s^2*T)", "s_max_rel_above_50pct": s,
+                               "T_s": dev_ms / 1000.0},
+                "latency_ms_per_step": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
+                "per_history": {"events": evs / (args.steps * H), "voxel_steps": geo / (args.steps * H),
+                                "deposits": dep / (args.steps * H), "algorithmic_bytes": per_hist_bytes},
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "peak_kind": peak_kind,
+                             "traffic": (traffic_ph * H) if traffic_ph else None,
+                             "kernel": "transport_kernel<float>",
+                             "atomics_per_s": dep / (dev_ms / 1000.0)},
+                "cpu_baseline": cpu,
+                "e2e": {"value": e2e_value, "unit": "histories/s", "h2d_bytes_per_step": int(h2d),
+                        "d2h_bytes_per_step": int(d2h)},
+                "gpu_launches": launches,
+                "clocks": clocks,
+            }
+        eng.close()
+        del regs
+        return line
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--histories-per-step", type=int, default=HISTORIES_PER_STEP,
+                    help="smaller values only for profiler captures of the same code path")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference_arm(args, rank)
+        return
+    dist_on = world > 1
+    if dist_on:
+        import torch.distributed as tdist
+
+        tdist.init_process_group("nccl")
+    line = run_ours(args, rank, world, local_rank, dist_on)
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+    if dist_on:
+        import torch.distributed as tdist
+
+        tdist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -245,6 +245,10 @@ typedef struct omc_run_config {
     int stack_depth;     /* per-lane particle stack; 0 = default          */
     int serial;          /* 1 = one lane, one stream: the reference's
                             serial build, history order included          */
+    int continue_streams;/* 1 = keep the RANMAR streams where the previous
+                            run of this engine left them (same lane count),
+                            as successive batches of one reference job;
+                            0 = seed them from (ixx, jxx)                  */
 } omc_run_config;
 
 typedef struct omc_run_stats {
@@ -254,6 +258,9 @@ typedef struct omc_run_stats {
     long long steps;       /* particle events processed                   */
     int max_stack;         /* deepest per-lane stack seen                 */
     int error_flags;       /* OR of device error bits (0 = clean)         */
+    long long voxel_steps; /* geometry steps (howfar calls)               */
+    long long deposits;    /* energy deposits (ausgab calls)              */
+    double kernel_ms;      /* device time of the transport + batch kernels */
 } omc_run_stats;
 
 omc_status omc_engine_create(int device, omc_engine **out);

@@ -184,22 +184,26 @@ class Engine:
     def load(self, problem: Problem):
         L = N.lib()
         check(L.omc_engine_set_tables(self._h, problem.tables))
-        check(L.omc_engine_set_geometry(self._h, problem.phantom._p, problem.regions))
+        self.set_geometry(problem)
         check(L.omc_engine_set_source(self._h, problem.source))
         self._problem = problem
         return self
 
+    def set_geometry(self, problem: Problem):
+        check(N.lib().omc_engine_set_geometry(self._h, problem.phantom._p, problem.regions))
+
     @staticmethod
-    def config(nperbatch, nbatch, seeds=(97, 33), nsplit=1, precision=FP64, nlanes=0, stack_depth=0, serial=0):
+    def config(nperbatch, nbatch, seeds=(97, 33), nsplit=1, precision=FP64, nlanes=0, stack_depth=0, serial=0,
+               continue_streams=0):
         return N.RunConfig_t(int(nperbatch), int(nbatch), int(seeds[0]), int(seeds[1]), int(nsplit),
-                             int(precision), int(nlanes), int(stack_depth), int(serial))
+                             int(precision), int(nlanes), int(stack_depth), int(serial), int(continue_streams))
 
     def run(self, nperbatch=None, nbatch=None, seeds=None, nsplit=None, precision=FP64, nlanes=0,
-            stack_depth=0, serial=0):
+            stack_depth=0, serial=0, continue_streams=0):
         p = self._problem
         cfg = self.config(p.nperbatch if nperbatch is None else nperbatch, p.nbatch if nbatch is None else nbatch,
                           p.seeds if seeds is None else seeds, p.nsplit if nsplit is None else nsplit,
-                          precision, nlanes, stack_depth, serial)
+                          precision, nlanes, stack_depth, serial, continue_streams)
         a = np.zeros(p.nreg)
         a2 = np.zeros(p.nreg)
         st = N.RunStats_t()

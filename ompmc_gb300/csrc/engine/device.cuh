@@ -115,6 +115,8 @@ struct Params {
   double *endep;             // [nreg] batch tally
   double *ensrc;             // [1]
   unsigned long long *events;
+  unsigned long long *n_geom;
+  unsigned long long *n_dep;
   int *max_np;
   unsigned *err;
 };

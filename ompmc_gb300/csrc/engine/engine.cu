@@ -96,6 +96,8 @@ __global__ void __launch_bounds__(kBlock) transport_kernel(Params<R> P) {
   P.rng_ijc[2 * P.nlanes + lane] = L.rng.c;
   atomicAdd(P.ensrc, L.ensrc);
   atomicAdd(P.events, events);
+  atomicAdd(P.n_geom, L.n_geom);
+  atomicAdd(P.n_dep, L.n_dep);
   atomicMax(P.max_np, L.max_np);
   if (L.err) atomicOr(P.err, L.err);
 }
@@ -182,7 +184,7 @@ struct omc_engine {
   int nreg = 0;
   // per-lane RNG state
   DevBuf rng_u, rng_ijc;
-  int seeded_lanes = 0, seeded_ixx = -1, seeded_jxx = -1;
+  int seeded_lanes = 0;  // lane count the current streams were seeded for
   // tallies and counters
   DevBuf endep, acc, acc2, counters;
   // host copies needed across uploads
@@ -194,6 +196,8 @@ namespace {
 struct Counters {
   unsigned long long next;
   unsigned long long events;
+  unsigned long long n_geom;
+  unsigned long long n_dep;
   double ensrc;
   int max_np;
   unsigned err;
@@ -372,6 +376,8 @@ omc_status run_batches(omc_engine *e, PrecisionState<R> &S, const omc_run_config
   P.endep = static_cast<double *>(e->endep.p);
   P.ensrc = &dc->ensrc;
   P.events = &dc->events;
+  P.n_geom = &dc->n_geom;
+  P.n_dep = &dc->n_dep;
   P.max_np = &dc->max_np;
   P.err = &dc->err;
   size_t smem = static_cast<size_t>(RNG_WORDS) * kBlock * sizeof(int);
@@ -404,6 +410,9 @@ omc_status run_batches(omc_engine *e, PrecisionState<R> &S, const omc_run_config
     stats->transport_ms = ms;
     stats->histories = cfg->nperbatch * cfg->nbatch;
     stats->steps = static_cast<long long>(hc.events);
+    stats->voxel_steps = static_cast<long long>(hc.n_geom);
+    stats->deposits = static_cast<long long>(hc.n_dep);
+    stats->kernel_ms = ms;
     stats->max_stack = hc.max_np + 1;
     stats->error_flags = static_cast<int>(hc.err);
   }
@@ -544,10 +553,16 @@ static omc_status engine_run(omc_engine *e, const omc_run_config *cfg, omc_run_s
   int nlanes = cfg->serial ? 1 : (cfg->nlanes > 0 ? cfg->nlanes : default_lanes(e));
   int depth = cfg->stack_depth > 0 ? cfg->stack_depth : kDefaultDepth + 4 * std::max(1, cfg->nsplit);
   // RANMAR streams, one per lane, seeded for this run.
-  if ((s = e->rng_u.ensure(static_cast<size_t>(RNG_WORDS) * nlanes * sizeof(int))) != OMC_OK) return s;
+  size_t rng_bytes = static_cast<size_t>(RNG_WORDS) * nlanes * sizeof(int);
+  if (e->rng_u.n < rng_bytes) e->seeded_lanes = 0;  // reallocated: streams must be seeded
+  if ((s = e->rng_u.ensure(rng_bytes)) != OMC_OK) return s;
   if ((s = e->rng_ijc.ensure(static_cast<size_t>(3) * nlanes * sizeof(int))) != OMC_OK) return s;
-  seed_kernel<<<(nlanes + 255) / 256, 256, 0, e->stream>>>(cfg->ixx, cfg->jxx, nlanes, static_cast<int *>(e->rng_u.p),
-                                                          static_cast<int *>(e->rng_ijc.p));
+  if (!(cfg->continue_streams && e->seeded_lanes == nlanes)) {
+    seed_kernel<<<(nlanes + 255) / 256, 256, 0, e->stream>>>(cfg->ixx, cfg->jxx, nlanes,
+                                                            static_cast<int *>(e->rng_u.p),
+                                                            static_cast<int *>(e->rng_ijc.p));
+    e->seeded_lanes = nlanes;
+  }
   cudaMemsetAsync(e->endep.p, 0, e->nreg * sizeof(double), e->stream);
   cudaMemsetAsync(e->acc.p, 0, e->nreg * sizeof(double), e->stream);
   cudaMemsetAsync(e->acc2.p, 0, e->nreg * sizeof(double), e->stream);

@@ -31,6 +31,8 @@ struct Lane {
   double ensrc;
   unsigned err;
   int max_np;
+  unsigned long long n_geom;  // howfar calls (voxel-stepping decisions)
+  unsigned long long n_dep;   // ausgab calls (energy deposits)
 
   __device__ Lane(const Params<R> &prm, int ln, int *su, int sstride) : P(prm), lane(ln) {
     rng.u = su;
@@ -39,6 +41,8 @@ struct Lane {
     ensrc = 0.0;
     err = 0;
     max_np = 0;
+    n_geom = 0;
+    n_dep = 0;
   }
 
   __device__ __forceinline__ R rnd() { return static_cast<R>(rng.next_int()) * RC(1.0 / 16777216.0); }
@@ -96,6 +100,7 @@ struct Lane {
 
   // ---- scoring: ausgab (omc_dosxyz.c:683-694) ------------------------------
   __device__ __forceinline__ void ausgab(int ir, R wt, R edep) {
+    n_dep++;
     atomicAdd(P.endep + ir, static_cast<double>(wt * edep));
   }
 
@@ -105,8 +110,9 @@ struct Lane {
   __device__ __forceinline__ R ecut_of(int ir) const { return __ldg(P.G.ecut_m + P.G.med[ir] + 1); }
   __device__ __forceinline__ R pcut_of(int ir) const { return __ldg(P.G.pcut_m + P.G.med[ir] + 1); }
 
-  __device__ void howfar(const Particle<R> &q, int &idisc, int &irnew, R &ustep) const {
+  __device__ void howfar(const Particle<R> &q, int &idisc, int &irnew, R &ustep) {
     const Geometry<R> &g = P.G;
+    n_geom++;
     int irl = q.ir;
     if (irl == 0) {
       idisc = 1;

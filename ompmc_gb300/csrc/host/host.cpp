@@ -255,7 +255,7 @@ extern "C" omc_status omc_phantom_write(const omc_phantom *ph, const char *path)
     for (int j = 0; j < ph->ny; j++) {
       for (int i = 0; i < ph->nx; i++) {
         size_t v = i + static_cast<size_t>(j) * ph->nx + static_cast<size_t>(k) * ph->nx * ph->ny;
-        std::fprintf(f, "%.9g ", ph->density[v]);
+        std::fprintf(f, "%.17g ", ph->density[v]);
       }
       std::fprintf(f, "\n");
     }

@@ -1,0 +1,67 @@
+"""Small dose jobs shared by the golden-fixture generator and the tests.
+
+Every case is a complete omc_dosxyz input (phantom, source, cuts, seeds),
+written from the seeded generators of ompmc_gb300.workloads, small enough
+for the serial oracle to finish in well under a second.
+"""
+
+from __future__ import annotations
+
+import os
+
+from ompmc_gb300 import data
+from ompmc_gb300 import workloads as W
+
+SLAB4 = ((0.0, 5.0, W.WATER, 1.0), (5.0, 15.0, W.LUNG, 0.26), (15.0, 18.0, W.BONE, 1.85),
+         (18.0, 30.0, W.AIR, 0.0012))
+
+# name -> (phantom builder, job keyword arguments)
+CASES = {
+    # 1.25 MeV parallel beam on water (the plain small configuration, coarse).
+    "water_mono": (lambda: W.homogeneous(n=12, vox=2.5),
+                   dict(mono_energy=1.25, ncase=2000, ssd=1e8)),
+    # Synthetic 6 MV point source on a four-medium slab.
+    "slab_6mv": (lambda: W.slab(n=20, vox=1.5, layers=SLAB4),
+                 dict(spectrum="6mv", ncase=2000, ssd=100.0)),
+    # 5 MeV electron pencil beam.
+    "electron_pencil": (lambda: W.homogeneous(n=12, vox=0.5),
+                        dict(mono_energy=5.0, charge=-1, collimator=(0.0, 0.0, 0.0, 0.0), ncase=500, ssd=100.0)),
+    # 5 MeV positrons, 2x2 cm field.
+    "positron_field": (lambda: W.homogeneous(n=12, vox=0.5),
+                       dict(mono_energy=5.0, charge=1, collimator=(-1.0, 1.0, -1.0, 1.0), ncase=500, ssd=100.0)),
+    # Photon splitting (nsplit = 10) with the 6 MV slab.
+    "slab_split10": (lambda: W.slab(n=20, vox=1.5, layers=SLAB4),
+                     dict(spectrum="6mv", ncase=1000, ssd=100.0, nsplit=10)),
+    # 250 kVp spectrum on the slab (photo-electric dominated).
+    "slab_250kvp": (lambda: W.slab(n=20, vox=1.5, layers=SLAB4),
+                    dict(spectrum="250kvp", ncase=2000, ssd=100.0)),
+}
+
+
+def write_case(name: str, directory: str, ncase: int | None = None, nbatch: int = 10, seeds=(97, 33)) -> str:
+    """Write the case's .egsphant/.spectrum/.inp into directory; returns the
+    input path without the .inp extension."""
+    builder, kw = CASES[name]
+    kw = dict(kw)
+    os.makedirs(directory, exist_ok=True)
+    P = data.paths()
+    ph = builder()
+    phant = os.path.join(directory, name + ".egsphant")
+    W.write_egsphant(ph, phant)
+    spec = kw.pop("spectrum", None)
+    spectrum_file = None
+    if spec == "6mv":
+        spectrum_file = W.write_spectrum(os.path.join(directory, name + ".spectrum"), "synthetic 6 MV",
+                                         *W.spectrum_6mv())
+    elif spec == "250kvp":
+        spectrum_file = W.write_spectrum(os.path.join(directory, name + ".spectrum"), "synthetic 250 kVp",
+                                         *W.spectrum_250kvp())
+    if ncase is not None:
+        kw["ncase"] = ncase
+    job = W.Job(phant, P["pegs"], P["pgs4form"], P["data_folder"], directory + os.sep,
+                spectrum_file=spectrum_file, nbatch=nbatch, seeds=seeds, **kw)
+    return job.write(os.path.join(directory, name))
+
+
+RANMAR_SEEDS = [(97, 33), (97, 34), (1802, 9373), (12, 31328), (31328, 1), (5, 17)]
+RANMAR_N = 2000

@@ -1,0 +1,118 @@
+"""GPU transport against the reference: RANMAR bit-exactness, trajectory
+parity of the serial lane with the reference's serial build (golden
+fixtures), and statistical parity of the many-lane FP64 and FP32 paths with
+the oracle.  All calls go through the C ABI."""
+
+import os
+
+import numpy as np
+import pytest
+from cases import CASES, RANMAR_N, RANMAR_SEEDS
+from conftest import GOLDEN
+from stats import compare
+
+from ompmc_gb300 import api
+
+pytestmark = pytest.mark.gpu
+
+
+def test_ranmar_streams_bit_exact(native):
+    g = np.load(os.path.join(GOLDEN, "ranmar.npz"))
+    for a, b in RANMAR_SEEDS:
+        out = api.gpu_ranmar(a, b, 1, RANMAR_N)
+        np.testing.assert_array_equal(out[0], g[f"{a}_{b}"], err_msg=f"seeds {a} {b}")
+
+
+def test_ranmar_lane_streams_follow_thread_seeding(native, oracle):
+    # lane k = the reference's OpenMP thread k: seeds (ixx, jxx + k); past
+    # jxx = 31328 the pair continues into ixx + 1.
+    out = api.gpu_ranmar(97, 31320, 20, 300)
+    for k in range(20):
+        ik, jk = api.stream_seeds(97, 31320, k)
+        np.testing.assert_array_equal(out[k], oracle.ranmar(ik, jk, 300))
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_serial_lane_reproduces_reference_trajectories(name, engine, problem_factory):
+    """One lane, one stream, histories in order: the reference's serial
+    build.  FP64 transport follows the same trajectories; only the last
+    bits of CUDA's math functions against the host libm differ."""
+    g = np.load(os.path.join(GOLDEN, f"dose_{name}.npz"))
+    prob = problem_factory(name)
+    engine.load(prob)
+    a, a2, st = engine.run(precision=api.FP64, serial=1)
+    assert st.error_flags == 0
+    ref = g["accum_endep"]
+    assert abs(st.ensrc - g["ensrc"][0]) <= 1e-9 * g["ensrc"][0]
+    np.testing.assert_allclose(a[1:].sum(), ref[1:].sum(), rtol=1e-8)
+    np.testing.assert_allclose(a, ref, rtol=1e-7, atol=1e-9 * ref.max())
+    np.testing.assert_allclose(a2, g["accum_endep2"], rtol=1e-6, atol=1e-9 * g["accum_endep2"].max())
+
+
+PARITY = [("water_mono", 400000), ("slab_6mv", 400000), ("slab_250kvp", 400000), ("electron_pencil", 40000),
+          ("positron_field", 40000), ("slab_split10", 40000)]
+
+
+@pytest.mark.parametrize("name,ncase", PARITY)
+@pytest.mark.parametrize("precision", [api.FP64, api.FP32])
+def test_many_lanes_statistically_identical(name, ncase, precision, engine, oracle, problem_factory):
+    """Per-voxel z-scores of the GPU against the OpenMP-seeded oracle over
+    voxels above 20% of Dmax (50 batches): |z| <= 2 for at least 93% of
+    them (95.4% expected), mean z^2 near 1, total energy within 1%."""
+    prob = problem_factory(name, ncase=ncase, nbatch=50, seeds=(33, 97))
+    engine.load(prob)
+    g, g2, st = engine.run(precision=precision)
+    assert st.error_flags == 0
+    o, o2, res = oracle.run(prob, nthreads=0)
+    c = compare(g, g2, o, o2, prob.nbatch)
+    assert c["n"] >= 20, c
+    assert c["frac_2sigma"] >= 0.93, c
+    assert 0.7 <= c["mean_z2"] <= 1.35, c
+    assert abs(c["etot_rel"]) < 0.01, c
+    if prob.source.contents.spectrum == 0:
+        assert st.ensrc == pytest.approx(res.ensrc, rel=1e-12)
+    else:
+        assert st.ensrc == pytest.approx(res.ensrc, rel=0.01)
+
+
+def test_fp32_against_fp64_on_the_gpu(engine, problem_factory):
+    """The FP32-transport dose error, stated against an FP64 run of the same
+    engine: statistically indistinguishable."""
+    prob = problem_factory("slab_6mv", ncase=400000, nbatch=50, seeds=(7, 11))
+    engine.load(prob)
+    d, d2, _ = engine.run(precision=api.FP64)
+    f, f2, _ = engine.run(precision=api.FP32)
+    c = compare(f, f2, d, d2, prob.nbatch)
+    assert c["frac_2sigma"] >= 0.93 and 0.7 <= c["mean_z2"] <= 1.35, c
+    assert abs(c["etot_rel"]) < 0.01, c
+
+
+def test_energy_balance_closes(engine, problem_factory):
+    """Energy deposited inside plus energy scored outside (region 0) cannot
+    exceed the source energy."""
+    prob = problem_factory("electron_pencil", ncase=20000)
+    engine.load(prob)
+    for prec in (api.FP64, api.FP32):
+        a, _, st = engine.run(precision=prec)
+        assert a.sum() <= st.ensrc * (1 + 1e-6)
+        assert a[1:].sum() > 0.5 * st.ensrc
+
+
+def test_results_independent_of_lane_count(engine, problem_factory):
+    prob = problem_factory("water_mono", ncase=200000, nbatch=50, seeds=(3, 4))
+    engine.load(prob)
+    a, a2, _ = engine.run(precision=api.FP32, nlanes=4096)
+    b, b2, _ = engine.run(precision=api.FP32)
+    c = compare(a, a2, b, b2, prob.nbatch)
+    assert c["frac_2sigma"] >= 0.93 and abs(c["etot_rel"]) < 0.01, c
+
+
+def test_reproducible_for_fixed_seeds_and_lanes(engine, problem_factory):
+    """Same seeds, same lane count: the same per-lane streams; the history
+    hand-out order can differ between runs, so only statistics are fixed,
+    but the serial lane is exactly reproducible."""
+    prob = problem_factory("slab_6mv")
+    engine.load(prob)
+    a, _, _ = engine.run(precision=api.FP64, serial=1)
+    b, _, _ = engine.run(precision=api.FP64, serial=1)
+    np.testing.assert_array_equal(a, b)
