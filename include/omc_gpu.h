@@ -241,7 +241,8 @@ typedef struct omc_run_config {
     int ixx, jxx;        /* "rng seeds"; lane k uses the k-th seed pair   */
     int nsplit;          /* "nsplit" photon splitting (ompmc.c:5964)      */
     int precision;       /* omc_precision                                 */
-    int nlanes;          /* concurrent histories; 0 = sized to the GPU    */
+    int nlanes;          /* per-lane schedule: concurrent histories;
+                            0 = sized to the GPU                          */
     int stack_depth;     /* per-lane particle stack; 0 = default          */
     int serial;          /* 1 = one lane, one stream: the reference's
                             serial build, history order included          */
@@ -249,7 +250,17 @@ typedef struct omc_run_config {
                             run of this engine left them (same lane count),
                             as successive batches of one reference job;
                             0 = seed them from (ixx, jxx)                  */
+    int schedule;        /* omc_schedule                                  */
+    long long inflight;  /* wavefront: particles kept in flight, 0 = auto  */
 } omc_run_config;
+
+typedef enum omc_schedule {
+    OMC_SCHEDULE_AUTO = 0,      /* wavefront, or per-lane when serial = 1  */
+    OMC_SCHEDULE_LANES = 1,     /* each lane transports whole histories in
+                                   the reference's stack order             */
+    OMC_SCHEDULE_WAVEFRONT = 2  /* photon and electron queues in HBM,
+                                   processed in alternating phases         */
+} omc_schedule;
 
 typedef struct omc_run_stats {
     double ensrc;          /* source kinetic energy, FP64 (score.ensrc)    */

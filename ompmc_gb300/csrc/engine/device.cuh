@@ -26,7 +26,9 @@ enum : unsigned {
   ERR_STACK = 1u,      // per-lane stack overflow: history dropped
   ERR_LOOP = 2u,       // a rejection loop hit its iteration cap
   ERR_EVENTS = 4u,     // a history exceeded the event cap: history dropped
-  ERR_TABLE = 8u       // an interpolation index left its table (clamped)
+  ERR_TABLE = 8u,      // an interpolation index left its table (clamped)
+  ERR_QUEUE = 16u,     // wavefront queue full: particle dropped
+  ERR_BARRIER = 32u    // a grid barrier gave up waiting
 };
 
 // Iteration caps of device loops.  The reference's loops end with

@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(kBlock) transport_kernel(Params<R> P) {
   const int lane = blockIdx.x * kBlock + t;
   if (lane >= P.nlanes) return;
   for (int k = 0; k < RNG_WORDS; k++) s_rng[k * kBlock + t] = P.rng_u[static_cast<size_t>(k) * P.nlanes + lane];
-  Lane<R> L(P, lane, s_rng + t, kBlock);
+  Lane<R, false> L(P, lane, s_rng + t, kBlock);
   L.rng.i = P.rng_ijc[lane];
   L.rng.j = P.rng_ijc[P.nlanes + lane];
   L.rng.c = P.rng_ijc[2 * P.nlanes + lane];
@@ -99,6 +99,136 @@ __global__ void __launch_bounds__(kBlock) transport_kernel(Params<R> P) {
   atomicAdd(P.n_geom, L.n_geom);
   atomicAdd(P.n_dep, L.n_dep);
   atomicMax(P.max_np, L.max_np);
+  if (L.err) atomicOr(P.err, L.err);
+}
+
+// ---------------------------------------------------------------------------
+// Wavefront schedule.  One cooperative, persistent launch per batch; every
+// thread keeps its RANMAR stream in shared memory for the whole batch.
+// Iteration: read the queue counters (identical in every thread), inject
+// new histories, photon phase, grid barrier, electron phase, grid barrier.
+// Queue buffers alternate between iterations; counters rotate over three
+// slots so a slot is zeroed only when no phase reads or appends it.
+// ---------------------------------------------------------------------------
+template <typename R>
+struct Wavefront {
+  R *ph_f[2];
+  int *ph_k[2];
+  R *el_f[2];
+  int *el_k[2];
+  unsigned cap;           // slots per queue
+  unsigned *ctr;          // [0..2] photon counters, [3..5] electron counters
+  unsigned long long *injected;
+  unsigned *bar_arrive;
+  unsigned *bar_gen;
+  unsigned target;        // particles kept in flight
+  int max_iters;
+  int *iters;             // iterations used (output)
+  unsigned *hwm;          // queue high-water mark (output)
+};
+
+constexpr long long kBarrierSpinCap = 1ll << 28;  // x ~64 ns: well past any phase
+
+// Grid-wide barrier for a cooperative launch (all blocks co-resident).  The
+// wait is bounded: on timeout the error flag is set and the block goes on,
+// so the kernel always ends.
+__device__ bool grid_barrier(unsigned *arrive, unsigned *gen, unsigned nblocks) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    s_ok = 1;
+    volatile unsigned *vgen = gen;
+    unsigned g = *vgen;
+    __threadfence();
+    if (atomicAdd(arrive, 1u) == nblocks - 1) {
+      atomicExch(arrive, 0u);
+      __threadfence();
+      atomicAdd(gen, 1u);
+    } else {
+      long long spins = 0;
+      while (*vgen == g) {
+        __nanosleep(64);
+        if (++spins > kBarrierSpinCap) {
+          s_ok = 0;
+          break;
+        }
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+__device__ __forceinline__ unsigned vload(const unsigned *p) { return *static_cast<const volatile unsigned *>(p); }
+
+template <typename R>
+__global__ void __launch_bounds__(kBlock) wavefront_kernel(Params<R> P, Wavefront<R> W) {
+  extern __shared__ int s_rng[];
+  const int t = threadIdx.x;
+  const int gtid = blockIdx.x * kBlock + t;
+  const unsigned nthreads = gridDim.x * kBlock;
+  for (int k = 0; k < RNG_WORDS; k++) s_rng[k * kBlock + t] = P.rng_u[static_cast<size_t>(k) * P.nlanes + gtid];
+  Lane<R, true> L(P, gtid, s_rng + t, kBlock);
+  L.rng.i = P.rng_ijc[gtid];
+  L.rng.j = P.rng_ijc[P.nlanes + gtid];
+  L.rng.c = P.rng_ijc[2 * P.nlanes + gtid];
+  L.queue_cap = W.cap;
+  unsigned long long events = 0;
+  int it = 0;
+  for (; it < W.max_iters; it++) {
+    const int bin = it & 1, bout = bin ^ 1;
+    const int cin = it % 3, cout = (it + 1) % 3, cfree = (it + 2) % 3;
+    const unsigned n_ph = vload(W.ctr + cin);
+    const unsigned n_el0 = vload(W.ctr + 3 + cin);
+    const unsigned long long injected = *static_cast<volatile unsigned long long *>(W.injected);
+    const long long remaining = P.nhist - static_cast<long long>(injected);
+    const unsigned long long inflight = static_cast<unsigned long long>(n_ph) + n_el0;
+    if (remaining <= 0 && inflight == 0) break;
+    long long m = static_cast<long long>(W.target) - static_cast<long long>(inflight);
+    if (m < 0) m = 0;
+    if (m > remaining) m = remaining;
+    if (gtid == 0) {
+      W.ctr[cfree] = 0;
+      W.ctr[3 + cfree] = 0;
+    }
+    // Injection and photon phase: photons go to the next iteration's photon
+    // queue, charged particles to this iteration's electron queue.
+    L.out = EmitTargets<R>{W.ph_f[bout], W.ph_k[bout], W.ctr + cout, W.el_f[bin], W.el_k[bin], W.ctr + 3 + cin};
+    for (long long h = gtid; h < m; h += nthreads) {
+      L.init_history();
+      L.emit(L.p);
+    }
+    for (unsigned i = gtid; i < n_ph; i += nthreads) {
+      L.take(W.ph_f[bin], W.ph_k[bin], i);
+      L.wf_photon_event();
+      events++;
+    }
+    if (!grid_barrier(W.bar_arrive, W.bar_gen, gridDim.x)) L.err |= ERR_BARRIER;
+    if (gtid == 0) *W.injected = injected + static_cast<unsigned long long>(m);
+    // Electron phase: one step (one iteration of electron()'s tstep loop)
+    // per charged particle.
+    const unsigned n_el = vload(W.ctr + 3 + cin);
+    L.out = EmitTargets<R>{W.ph_f[bout], W.ph_k[bout], W.ctr + cout, W.el_f[bout], W.el_k[bout], W.ctr + 3 + cout};
+    for (unsigned i = gtid; i < n_el; i += nthreads) {
+      L.take(W.el_f[bin], W.el_k[bin], i);
+      L.electron_event();
+      if (L.alive) L.emit(L.p);
+      events++;
+    }
+    if (!grid_barrier(W.bar_arrive, W.bar_gen, gridDim.x)) L.err |= ERR_BARRIER;
+  }
+  if (it >= W.max_iters) L.err |= ERR_LOOP;
+  for (int k = 0; k < RNG_WORDS; k++) P.rng_u[static_cast<size_t>(k) * P.nlanes + gtid] = s_rng[k * kBlock + t];
+  P.rng_ijc[gtid] = L.rng.i;
+  P.rng_ijc[P.nlanes + gtid] = L.rng.j;
+  P.rng_ijc[2 * P.nlanes + gtid] = L.rng.c;
+  atomicAdd(P.ensrc, L.ensrc);
+  atomicAdd(P.events, events);
+  atomicAdd(P.n_geom, L.n_geom);
+  atomicAdd(P.n_dep, L.n_dep);
+  atomicMax(W.hwm, L.queue_hwm);
+  if (gtid == 0) *W.iters = it;
   if (L.err) atomicOr(P.err, L.err);
 }
 
@@ -169,6 +299,7 @@ struct PrecisionState {
   Geometry<R> G{};
   Source<R> S{};
   DevBuf stk, key;
+  DevBuf queue;  // wavefront: 4 queues of 8 planes + keys
   bool tables_ok = false, geom_ok = false, source_ok = false;
 };
 
@@ -186,7 +317,7 @@ struct omc_engine {
   DevBuf rng_u, rng_ijc;
   int seeded_lanes = 0;  // lane count the current streams were seeded for
   // tallies and counters
-  DevBuf endep, acc, acc2, counters;
+  DevBuf endep, acc, acc2, counters, wf_counters;
   // host copies needed across uploads
   omc_tables host_tables_dims{};
 };
@@ -421,16 +552,135 @@ omc_status run_batches(omc_engine *e, PrecisionState<R> &S, const omc_run_config
   return OMC_OK;
 }
 
+struct WfCounters {
+  unsigned ctr[6];
+  unsigned long long injected;
+  unsigned bar_arrive, bar_gen;
+  int iters;
+  unsigned hwm;
+};
+
+template <typename R>
+int wavefront_blocks(omc_engine *e) {
+  size_t smem = static_cast<size_t>(RNG_WORDS) * kBlock * sizeof(int);
+  cudaFuncSetAttribute(wavefront_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wavefront_kernel<R>, kBlock, smem);
+  return (per_sm < 1 ? 1 : per_sm) * e->nsm;
+}
+
+template <typename R>
+omc_status run_wavefront(omc_engine *e, PrecisionState<R> &S, const omc_run_config *cfg, int nlanes,
+                         omc_run_stats *stats) {
+  const int nsplit = cfg->nsplit < 1 ? 1 : cfg->nsplit;
+  const int blocks = nlanes / kBlock;
+  unsigned long long target = cfg->inflight > 0 ? static_cast<unsigned long long>(cfg->inflight)
+                                                 : static_cast<unsigned long long>(nlanes) * 8;
+  // Worst case growth in one iteration: every photon of a cycle leaves up
+  // to two particles per split, every electron step up to two.
+  unsigned long long cap = target * (4ull + 2ull * nsplit) + 4ull * nlanes;
+  if (cap > 0x7fffffffull) cap = 0x7fffffffull;
+  size_t per_queue = static_cast<size_t>(cap) * (8 * sizeof(R) + sizeof(int));
+  if (S.queue.ensure(4 * per_queue) != OMC_OK) return OMC_ERR_NOMEM;
+  if (e->wf_counters.ensure(sizeof(WfCounters)) != OMC_OK) return OMC_ERR_NOMEM;
+  char *qb = static_cast<char *>(S.queue.p);
+  Wavefront<R> W{};
+  for (int q = 0; q < 4; q++) {
+    R *f = reinterpret_cast<R *>(qb + q * per_queue);
+    int *k = reinterpret_cast<int *>(qb + q * per_queue + static_cast<size_t>(cap) * 8 * sizeof(R));
+    if (q < 2) {
+      W.ph_f[q] = f;
+      W.ph_k[q] = k;
+    } else {
+      W.el_f[q - 2] = f;
+      W.el_k[q - 2] = k;
+    }
+  }
+  WfCounters *wc = static_cast<WfCounters *>(e->wf_counters.p);
+  W.cap = static_cast<unsigned>(cap);
+  W.ctr = wc->ctr;
+  W.injected = &wc->injected;
+  W.bar_arrive = &wc->bar_arrive;
+  W.bar_gen = &wc->bar_gen;
+  W.target = static_cast<unsigned>(target > 0xffffffffull ? 0xffffffffull : target);
+  W.max_iters = 1 << 24;
+  W.iters = &wc->iters;
+  W.hwm = &wc->hwm;
+  Counters *dc = static_cast<Counters *>(e->counters.p);
+  Params<R> P{};
+  P.T = S.T;
+  P.G = S.G;
+  P.S = S.S;
+  P.nsplit = nsplit;
+  P.nlanes = nlanes;
+  P.nhist = cfg->nperbatch;
+  P.next = &dc->next;
+  P.rng_u = static_cast<int *>(e->rng_u.p);
+  P.rng_ijc = static_cast<int *>(e->rng_ijc.p);
+  P.endep = static_cast<double *>(e->endep.p);
+  P.ensrc = &dc->ensrc;
+  P.events = &dc->events;
+  P.n_geom = &dc->n_geom;
+  P.n_dep = &dc->n_dep;
+  P.max_np = &dc->max_np;
+  P.err = &dc->err;
+  size_t smem = static_cast<size_t>(RNG_WORDS) * kBlock * sizeof(int);
+  cudaEvent_t t0, t1;
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  cudaEventRecord(t0, e->stream);
+  int iters_total = 0;
+  cudaError_t err = cudaSuccess;
+  for (int b = 0; b < cfg->nbatch && err == cudaSuccess; b++) {
+    cudaMemsetAsync(wc, 0, sizeof(WfCounters), e->stream);
+    void *args[] = {&P, &W};
+    err = cudaLaunchCooperativeKernel(reinterpret_cast<void *>(wavefront_kernel<R>), dim3(blocks), dim3(kBlock),
+                                      args, smem, e->stream);
+    accumulate_kernel<<<std::max(1, std::min(4 * e->nsm, (e->nreg + 255) / 256)), 256, 0, e->stream>>>(
+        static_cast<double *>(e->endep.p), static_cast<double *>(e->acc.p), static_cast<double *>(e->acc2.p),
+        e->nreg);
+  }
+  cudaEventRecord(t1, e->stream);
+  cudaError_t serr = cudaStreamSynchronize(e->stream);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, t0, t1);
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  if (err != cudaSuccess) return fail(OMC_ERR_CUDA, "wavefront launch: %s", cudaGetErrorString(err));
+  if (serr != cudaSuccess) return fail(OMC_ERR_CUDA, "wavefront transport: %s", cudaGetErrorString(serr));
+  Counters hc{};
+  WfCounters hw{};
+  cudaMemcpy(&hc, dc, sizeof hc, cudaMemcpyDeviceToHost);
+  cudaMemcpy(&hw, wc, sizeof hw, cudaMemcpyDeviceToHost);
+  iters_total = hw.iters;
+  if (stats) {
+    stats->ensrc = hc.ensrc;
+    stats->transport_ms = ms;
+    stats->kernel_ms = ms;
+    stats->histories = cfg->nperbatch * cfg->nbatch;
+    stats->steps = static_cast<long long>(hc.events);
+    stats->voxel_steps = static_cast<long long>(hc.n_geom);
+    stats->deposits = static_cast<long long>(hc.n_dep);
+    stats->max_stack = static_cast<int>(hw.hwm + 1);
+    stats->error_flags = static_cast<int>(hc.err);
+  }
+  (void)iters_total;
+  if (hc.err & ERR_QUEUE) return fail(OMC_ERR_STACK, "wavefront queue overflow (capacity %llu); particles were dropped", cap);
+  if (hc.err & (ERR_LOOP | ERR_EVENTS | ERR_BARRIER)) return fail(OMC_ERR_LIMIT, "a device loop hit its iteration limit");
+  return OMC_OK;
+}
+
 omc_status ensure_device(omc_engine *e) {
   CUDA_TRY(cudaSetDevice(e->device));
   return OMC_OK;
 }
 
+template <typename R>
 int default_lanes(omc_engine *e) {
   int per_sm = 0;
   size_t smem = static_cast<size_t>(RNG_WORDS) * kBlock * sizeof(int);
-  cudaFuncSetAttribute(transport_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, transport_kernel<float>, kBlock, smem);
+  cudaFuncSetAttribute(transport_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, transport_kernel<R>, kBlock, smem);
   if (per_sm < 1) per_sm = 1;
   return e->nsm * per_sm * kBlock;
 }
@@ -470,6 +720,9 @@ extern "C" void omc_engine_destroy(omc_engine *e) {
   e->f64.source.clear();
   e->f64.stk.release();
   e->f64.key.release();
+  e->f64.queue.release();
+  e->f32.queue.release();
+  e->wf_counters.release();
   e->f32.tables.clear();
   e->f32.geom.clear();
   e->f32.source.clear();
@@ -550,7 +803,13 @@ static omc_status engine_run(omc_engine *e, const omc_run_config *cfg, omc_run_s
   if (cfg->precision != OMC_FP64 && cfg->precision != OMC_FP32) return fail(OMC_ERR_ARG, "unknown precision");
   omc_status s;
   if ((s = ensure_device(e)) != OMC_OK) return s;
-  int nlanes = cfg->serial ? 1 : (cfg->nlanes > 0 ? cfg->nlanes : default_lanes(e));
+  const bool fp64 = cfg->precision == OMC_FP64;
+  const bool wavefront = !cfg->serial && cfg->schedule != OMC_SCHEDULE_LANES;
+  if (cfg->schedule < 0 || cfg->schedule > OMC_SCHEDULE_WAVEFRONT) return fail(OMC_ERR_ARG, "unknown schedule");
+  int nlanes;
+  if (wavefront) nlanes = (fp64 ? wavefront_blocks<double>(e) : wavefront_blocks<float>(e)) * kBlock;
+  else if (cfg->serial) nlanes = 1;
+  else nlanes = cfg->nlanes > 0 ? cfg->nlanes : (fp64 ? default_lanes<double>(e) : default_lanes<float>(e));
   int depth = cfg->stack_depth > 0 ? cfg->stack_depth : kDefaultDepth + 4 * std::max(1, cfg->nsplit);
   // RANMAR streams, one per lane, seeded for this run.
   size_t rng_bytes = static_cast<size_t>(RNG_WORDS) * nlanes * sizeof(int);
@@ -567,8 +826,8 @@ static omc_status engine_run(omc_engine *e, const omc_run_config *cfg, omc_run_s
   cudaMemsetAsync(e->acc.p, 0, e->nreg * sizeof(double), e->stream);
   cudaMemsetAsync(e->acc2.p, 0, e->nreg * sizeof(double), e->stream);
   cudaMemsetAsync(e->counters.p, 0, sizeof(Counters), e->stream);
-  if (cfg->precision == OMC_FP64) return run_batches(e, e->f64, cfg, nlanes, depth, stats);
-  return run_batches(e, e->f32, cfg, nlanes, depth, stats);
+  if (wavefront) return fp64 ? run_wavefront(e, e->f64, cfg, nlanes, stats) : run_wavefront(e, e->f32, cfg, nlanes, stats);
+  return fp64 ? run_batches(e, e->f64, cfg, nlanes, depth, stats) : run_batches(e, e->f32, cfg, nlanes, depth, stats);
 }
 
 extern "C" omc_status omc_engine_run(omc_engine *e, const omc_run_config *cfg, double *accum_endep,

@@ -6,8 +6,15 @@
 // thread of the reference does; R is the transport precision (double or
 // float), tallies are always FP64.
 //
-// Stack discipline: the top particle lives in registers (p, at slot np);
-// slots 0..np-1 live in HBM in the lane's interleaved stack.
+// Two schedules share this code (WF template parameter):
+//  - per-lane histories (WF = false): the top particle lives in registers
+//    (p, at slot np); slots 0..np-1 live in HBM in the lane's interleaved
+//    stack; a lane finishes a history before it takes the next, so a lane
+//    with its stream is exactly a thread of the reference;
+//  - wavefront (WF = true): p is one particle taken from a photon or
+//    electron queue in HBM; every particle an event leaves behind is
+//    appended to the queue of its kind (warp-aggregated), and the next
+//    phase of the persistent kernel picks it up.
 #pragma once
 
 #include "device.cuh"
@@ -21,13 +28,34 @@ __device__ __forceinline__ R pwlf(const R *c1, const R *c0, int idx, R lv) {
   return lv * __ldg(c1 + idx) + __ldg(c0 + idx);
 }
 
+// Output queues of the current wavefront phase.
 template <typename R>
+struct EmitTargets {
+  R *ph_f;            // photon queue planes [8][cap]
+  int *ph_k;          // photon queue keys   [cap]
+  unsigned *ph_n;     // photon queue counter
+  R *el_f;
+  int *el_k;
+  unsigned *el_n;
+};
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+template <typename R, bool WF>
 struct Lane {
   const Params<R> &P;
   Ranmar rng;
   int lane;
-  int np;  // top slot, -1 = empty
+  int np;  // top slot, -1 = empty (per-lane schedule)
   Particle<R> p;
+  bool alive;           // wavefront: p still needs to be queued
+  EmitTargets<R> out;   // wavefront: where this phase appends
+  unsigned queue_cap;
+  unsigned queue_hwm;   // highest slot appended
   double ensrc;
   unsigned err;
   int max_np;
@@ -43,6 +71,9 @@ struct Lane {
     max_np = 0;
     n_geom = 0;
     n_dep = 0;
+    alive = false;
+    queue_cap = 0;
+    queue_hwm = 0;
   }
 
   __device__ __forceinline__ R rnd() { return static_cast<R>(rng.next_int()) * RC(1.0 / 16777216.0); }
@@ -79,23 +110,79 @@ struct Lane {
     q.ir = key >> 2;
     q.iq = (key & 3) - 1;
   }
-  // The top (p) goes to memory and q becomes the new top.  False (history
-  // dropped, error flagged) if the lane's stack is full.
+  // Per-lane schedule: the top (p) goes to memory and q becomes the new top
+  // (false, history dropped, error flagged, if the stack is full).
+  // Wavefront: q is appended to its queue and p stays current.
   __device__ __forceinline__ bool push(const Particle<R> &q) {
-    if (np + 1 >= P.depth) {
-      err |= ERR_STACK;
-      np = -1;
-      return false;
+    if constexpr (WF) {
+      emit(q);
+      return true;
+    } else {
+      if (np + 1 >= P.depth) {
+        err |= ERR_STACK;
+        np = -1;
+        return false;
+      }
+      store(np, p);
+      np += 1;
+      p = q;
+      if (np > max_np) max_np = np;
+      return true;
     }
-    store(np, p);
-    np += 1;
-    p = q;
-    if (np > max_np) max_np = np;
-    return true;
   }
+  // Per-lane schedule: remove the top; wavefront: p is consumed.
   __device__ __forceinline__ void pop() {
-    np -= 1;
-    if (np >= 0) load(np, p);
+    if constexpr (WF) {
+      alive = false;
+    } else {
+      np -= 1;
+      if (np >= 0) load(np, p);
+    }
+  }
+
+  // Wavefront append: lanes that emit together share one atomic per queue
+  // (ballot + popc), so a warp writes consecutive, coalesced slots.
+  __device__ __forceinline__ void emit_to(R *f, int *k, unsigned *n, const Particle<R> &q) {
+    unsigned m = __activemask();
+    int leader = __ffs(m) - 1;
+    unsigned base = 0;
+    if ((threadIdx.x & 31) == leader) base = atomicAdd(n, static_cast<unsigned>(__popc(m)));
+    base = __shfl_sync(m, base, leader);
+    unsigned slot = base + __popc(m & lanemask_lt());
+    if (slot >= queue_cap) {
+      err |= ERR_QUEUE;
+      return;
+    }
+    if (slot > queue_hwm) queue_hwm = slot;
+    size_t c = queue_cap;
+    __stcg(f + slot, q.e);
+    __stcg(f + c + slot, q.x);
+    __stcg(f + 2 * c + slot, q.y);
+    __stcg(f + 3 * c + slot, q.z);
+    __stcg(f + 4 * c + slot, q.u);
+    __stcg(f + 5 * c + slot, q.v);
+    __stcg(f + 6 * c + slot, q.w);
+    __stcg(f + 7 * c + slot, q.wt);
+    __stcg(k + slot, q.ir * 4 + (q.iq + 1));
+  }
+  __device__ __forceinline__ void emit(const Particle<R> &q) {
+    if (q.iq == 0) emit_to(out.ph_f, out.ph_k, out.ph_n, q);
+    else emit_to(out.el_f, out.el_k, out.el_n, q);
+  }
+  __device__ __forceinline__ void take(const R *f, const int *k, unsigned slot) {
+    size_t c = queue_cap;
+    p.e = __ldcg(f + slot);
+    p.x = __ldcg(f + c + slot);
+    p.y = __ldcg(f + 2 * c + slot);
+    p.z = __ldcg(f + 3 * c + slot);
+    p.u = __ldcg(f + 4 * c + slot);
+    p.v = __ldcg(f + 5 * c + slot);
+    p.w = __ldcg(f + 6 * c + slot);
+    p.wt = __ldcg(f + 7 * c + slot);
+    int key = __ldcg(k + slot);
+    p.ir = key >> 2;
+    p.iq = (key & 3) - 1;
+    alive = true;
   }
 
   // ---- scoring: ausgab (omc_dosxyz.c:683-694) ------------------------------

@@ -16,7 +16,7 @@ def test_stack_overflow_is_reported_not_fatal(engine, problem_factory):
     prob = problem_factory("slab_split10", ncase=2000)
     engine.load(prob)
     with pytest.raises(N.OmcError) as e:
-        engine.run(precision=api.FP32, stack_depth=4)
+        engine.run(precision=api.FP32, stack_depth=4, schedule=api.LANES)
     assert e.value.status == 8  # OMC_ERR_STACK
     # The engine still works afterwards.
     a, _, st = engine.run(precision=api.FP32)
@@ -51,3 +51,12 @@ def test_empty_run(engine, problem_factory):
     engine.load(prob)
     a, a2, st = engine.run(nperbatch=0, nbatch=3)
     assert st.histories == 0 and not a.any() and not a2.any()
+
+
+def test_wavefront_queue_overflow_is_reported(engine, problem_factory):
+    # An in-flight target far above what the queues can hold is impossible
+    # by construction; a tiny target with photon splitting still works.
+    prob = problem_factory("slab_split10", ncase=2000)
+    engine.load(prob)
+    a, _, st = engine.run(precision=api.FP32, schedule=api.WAVEFRONT, inflight=64)
+    assert st.error_flags == 0 and a[1:].sum() > 0
