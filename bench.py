@@ -35,7 +35,7 @@ sys.path.insert(0, ROOT)
 
 WORKLOAD = "6MV heterogeneous slab 150^3 @ 2 mm, 10x10 cm2 field, SSD 100 cm"
 HISTORIES_PER_STEP = 10_000_000
-FP64_HISTORIES = 1_000_000
+FP64_HISTORIES = 4_000_000
 LANES_PER_RANK_STRIDE = 1 << 21  # stream-index stride between ranks (> lanes of one GPU)
 L2_FLUSH_BYTES = 256 << 20       # larger than the 129 MB L2
 

@@ -105,10 +105,11 @@ __global__ void __launch_bounds__(kBlock) transport_kernel(Params<R> P) {
 // ---------------------------------------------------------------------------
 // Wavefront schedule.  One cooperative, persistent launch per batch; every
 // thread keeps its RANMAR stream in shared memory for the whole batch.
-// Iteration: read the queue counters (identical in every thread), inject
-// new histories, photon phase, grid barrier, electron phase, grid barrier.
-// Queue buffers alternate between iterations; counters rotate over three
-// slots so a slot is zeroed only when no phase reads or appends it.
+// Iteration: read the queue counters (identical in every thread), then one
+// phase in which warps claim 32-wide chunks of [new histories | photons |
+// electrons] until none is left, then one grid barrier.  Queue buffers
+// alternate between iterations; counters rotate over three slots so a slot
+// is zeroed only when no phase reads or appends it.
 // ---------------------------------------------------------------------------
 template <typename R>
 struct Wavefront {
@@ -118,7 +119,8 @@ struct Wavefront {
   int *el_k[2];
   unsigned cap;           // slots per queue
   unsigned *ctr;          // [0..2] photon counters, [3..5] electron counters
-  unsigned long long *injected;
+  unsigned long long *work;      // [3] chunk counters of the phase
+  unsigned long long *injected;  // [2] histories injected before the iteration
   unsigned *bar_arrive;
   unsigned *bar_gen;
   unsigned target;        // particles kept in flight
@@ -167,7 +169,7 @@ __global__ void __launch_bounds__(kBlock) wavefront_kernel(Params<R> P, Wavefron
   extern __shared__ int s_rng[];
   const int t = threadIdx.x;
   const int gtid = blockIdx.x * kBlock + t;
-  const unsigned nthreads = gridDim.x * kBlock;
+  const int lane_id = t & 31;
   for (int k = 0; k < RNG_WORDS; k++) s_rng[k * kBlock + t] = P.rng_u[static_cast<size_t>(k) * P.nlanes + gtid];
   Lane<R, true> L(P, gtid, s_rng + t, kBlock);
   L.rng.i = P.rng_ijc[gtid];
@@ -179,11 +181,13 @@ __global__ void __launch_bounds__(kBlock) wavefront_kernel(Params<R> P, Wavefron
   for (; it < W.max_iters; it++) {
     const int bin = it & 1, bout = bin ^ 1;
     const int cin = it % 3, cout = (it + 1) % 3, cfree = (it + 2) % 3;
+    // Everything below is read after the last barrier, so every thread
+    // sees the same values and takes the same branches.
     const unsigned n_ph = vload(W.ctr + cin);
-    const unsigned n_el0 = vload(W.ctr + 3 + cin);
-    const unsigned long long injected = *static_cast<volatile unsigned long long *>(W.injected);
+    const unsigned n_el = vload(W.ctr + 3 + cin);
+    const unsigned long long injected = *static_cast<volatile unsigned long long *>(W.injected + bin);
     const long long remaining = P.nhist - static_cast<long long>(injected);
-    const unsigned long long inflight = static_cast<unsigned long long>(n_ph) + n_el0;
+    const unsigned long long inflight = static_cast<unsigned long long>(n_ph) + n_el;
     if (remaining <= 0 && inflight == 0) break;
     long long m = static_cast<long long>(W.target) - static_cast<long long>(inflight);
     if (m < 0) m = 0;
@@ -191,30 +195,44 @@ __global__ void __launch_bounds__(kBlock) wavefront_kernel(Params<R> P, Wavefron
     if (gtid == 0) {
       W.ctr[cfree] = 0;
       W.ctr[3 + cfree] = 0;
+      W.work[cfree] = 0;
+      W.injected[bout] = injected + static_cast<unsigned long long>(m);
     }
-    // Injection and photon phase: photons go to the next iteration's photon
-    // queue, charged particles to this iteration's electron queue.
-    L.out = EmitTargets<R>{W.ph_f[bout], W.ph_k[bout], W.ctr + cout, W.el_f[bin], W.el_k[bin], W.ctr + 3 + cin};
-    for (long long h = gtid; h < m; h += nthreads) {
-      L.init_history();
-      L.emit(L.p);
-    }
-    for (unsigned i = gtid; i < n_ph; i += nthreads) {
-      L.take(W.ph_f[bin], W.ph_k[bin], i);
-      L.wf_photon_event();
-      events++;
-    }
-    if (!grid_barrier(W.bar_arrive, W.bar_gen, gridDim.x)) L.err |= ERR_BARRIER;
-    if (gtid == 0) *W.injected = injected + static_cast<unsigned long long>(m);
-    // Electron phase: one step (one iteration of electron()'s tstep loop)
-    // per charged particle.
-    const unsigned n_el = vload(W.ctr + 3 + cin);
+    // One phase: new histories, then photons, then electrons, each range
+    // padded to a multiple of 32 so that a warp's chunk is one code path.
+    // Everything produced goes to the next iteration's queues.
     L.out = EmitTargets<R>{W.ph_f[bout], W.ph_k[bout], W.ctr + cout, W.el_f[bout], W.el_k[bout], W.ctr + 3 + cout};
-    for (unsigned i = gtid; i < n_el; i += nthreads) {
-      L.take(W.el_f[bin], W.el_k[bin], i);
-      L.electron_event();
-      if (L.alive) L.emit(L.p);
-      events++;
+    const unsigned long long m_pad = (static_cast<unsigned long long>(m) + 31) & ~31ull;
+    const unsigned long long ph_pad = (static_cast<unsigned long long>(n_ph) + 31) & ~31ull;
+    const unsigned long long total = m_pad + ph_pad + n_el;
+    for (;;) {
+      unsigned long long base = 0;
+      if (lane_id == 0) base = atomicAdd(W.work + cin, 32ull);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (base >= total) break;
+      const unsigned long long i = base + lane_id;
+      if (base < m_pad) {
+        if (i < static_cast<unsigned long long>(m)) {
+          L.init_history();
+          L.emit(L.p);
+        }
+      } else if (base < m_pad + ph_pad) {
+        const unsigned long long k = i - m_pad;
+        if (k < n_ph) {
+          L.take(W.ph_f[bin], W.ph_k[bin], static_cast<unsigned>(k));
+          L.wf_photon_event();
+          events++;
+        }
+      } else {
+        const unsigned long long k = i - m_pad - ph_pad;
+        if (k < n_el) {
+          // One step: one iteration of electron()'s tstep loop.
+          L.take(W.el_f[bin], W.el_k[bin], static_cast<unsigned>(k));
+          L.electron_event();
+          if (L.alive) L.emit(L.p);
+          events++;
+        }
+      }
     }
     if (!grid_barrier(W.bar_arrive, W.bar_gen, gridDim.x)) L.err |= ERR_BARRIER;
   }
@@ -554,7 +572,8 @@ omc_status run_batches(omc_engine *e, PrecisionState<R> &S, const omc_run_config
 
 struct WfCounters {
   unsigned ctr[6];
-  unsigned long long injected;
+  unsigned long long work[3];
+  unsigned long long injected[2];
   unsigned bar_arrive, bar_gen;
   int iters;
   unsigned hwm;
@@ -599,11 +618,12 @@ omc_status run_wavefront(omc_engine *e, PrecisionState<R> &S, const omc_run_conf
   WfCounters *wc = static_cast<WfCounters *>(e->wf_counters.p);
   W.cap = static_cast<unsigned>(cap);
   W.ctr = wc->ctr;
-  W.injected = &wc->injected;
+  W.work = wc->work;
+  W.injected = wc->injected;
   W.bar_arrive = &wc->bar_arrive;
   W.bar_gen = &wc->bar_gen;
   W.target = static_cast<unsigned>(target > 0xffffffffull ? 0xffffffffull : target);
-  W.max_iters = 1 << 24;
+  W.max_iters = 1 << 21;
   W.iters = &wc->iters;
   W.hwm = &wc->hwm;
   Counters *dc = static_cast<Counters *>(e->counters.p);

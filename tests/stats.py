@@ -31,3 +31,19 @@ def compare(acc_a, acc2_a, acc_b, acc2_b, nbatch, dmax_frac=0.2):
         "etot_b": float(acc_b[1:].sum()),
         "etot_rel": float((acc_a[1:].sum() - acc_b[1:].sum()) / acc_b[1:].sum()),
     }
+
+
+def consistent(c, p_min=1e-4):
+    """Two runs are statistically identical if the number of voxels with
+    |z| > 2 is plausible under Binomial(n, 0.0455) and sum z^2 under
+    chi^2(n), both at tail probability p_min (voxels are treated as
+    independent)."""
+    from scipy import stats as S
+
+    n = c["n"]
+    k_out = int(round((1.0 - c["frac_2sigma"]) * n))
+    p_binom = float(S.binom.sf(k_out - 1, n, 0.0455)) if k_out > 0 else 1.0
+    q = c["mean_z2"] * n
+    p_chi2 = float(min(S.chi2.cdf(q, n), S.chi2.sf(q, n)))
+    c["p_binom"], c["p_chi2"] = p_binom, p_chi2
+    return p_binom > p_min and p_chi2 > p_min

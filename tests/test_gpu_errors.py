@@ -53,7 +53,7 @@ def test_empty_run(engine, problem_factory):
     assert st.histories == 0 and not a.any() and not a2.any()
 
 
-def test_wavefront_queue_overflow_is_reported(engine, problem_factory):
+def test_wavefront_small_inflight_target(engine, problem_factory):
     # An in-flight target far above what the queues can hold is impossible
     # by construction; a tiny target with photon splitting still works.
     prob = problem_factory("slab_split10", ncase=2000)
