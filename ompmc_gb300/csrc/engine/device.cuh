@@ -46,11 +46,27 @@ struct Particle {
   int iq, ir;
 };
 
+// Four table values read together (one 16- or 32-byte load).
+template <typename R>
+struct alignas(4 * sizeof(R)) V4 {
+  R x, y, z, w;
+};
+
 // ---------------------------------------------------------------------------
-// Tables resident on the device, in the reference's index layout (the
-// arrays of omc_tables), converted to R.
+// Tables resident on the device, converted to R.  Scalar arrays keep the
+// reference's index layout (the arrays of omc_tables); the interpolation
+// coefficients read on every step are also packed per (medium, energy bin)
+// into V4 records so that a lookup is one load:
+//   ph_mfp [m][l] = {gmfp1, gmfp0, cohe1, cohe0}
+//   ph_br  [m][l] = {gbr11, gbr10, gbr21, gbr20}
+//   el_sd  [q][m][l] = {sig1, sig0, dedx1, dedx0}   (q = 0 e-, 1 e+)
+//   el_te  [q][m][l] = {tmxs1, tmxs0, eta1, eta0}
+//   el_rg  [q][m][l] = {blcce1, blcce0, range_ep, e_array}
+//   el_q   [q][m][l] = {q1c1, q1c0, q2c1, q2c0}
+//   el_ib  [m][l] = {ebr11, ebr10, pbr11, pbr10},  el_ib2 [m][l] = {pbr21, pbr20, 0, 0}
 template <typename R>
 struct Tables {
+  const V4<R> *ph_mfp, *ph_br, *el_sd, *el_te, *el_rg, *el_q, *el_ib, *el_ib2;
   int nmed;
   // per medium
   const R *ge0, *ge1, *eke0, *eke1, *xcc, *blcc, *te, *thmoll, *ap;
@@ -124,14 +140,47 @@ struct Params {
 };
 
 // ---------------------------------------------------------------------------
-// RANMAR (omc_random.c:58-187) with the 97-word state in shared memory,
-// word k of a thread at u[k*stride].  Numbers are produced one at a time;
-// the reference refills blocks of 128 but returns them in the same order.
+// RANMAR (omc_random.c:58-187) with the 97-word state in shared memory.
+// Every word is a 24-bit integer, kept as a 16-bit low plane and an 8-bit
+// high plane (3 bytes per word instead of 4, so more lanes fit on an SM);
+// word k of a thread sits at index k*stride of each plane.  Numbers are
+// produced one at a time; the reference refills blocks of 128 but returns
+// them in the same order.
 struct Ranmar {
-  int *u;
+  unsigned short *lo;
+  unsigned char *hi;
   int stride;
   int i, j, c;
 
+  __device__ __forceinline__ int word(int k) const {
+    return static_cast<int>(lo[k * stride]) | (static_cast<int>(hi[k * stride]) << 16);
+  }
+  __device__ __forceinline__ void set_word(int k, int v) {
+    lo[k * stride] = static_cast<unsigned short>(v & 0xffff);
+    hi[k * stride] = static_cast<unsigned char>(v >> 16);
+  }
+  __device__ __forceinline__ int next_int() {
+    int iopt = word(i - 1) - word(j - 1);
+    if (iopt < 0) iopt += 16777216;
+    set_word(i - 1, iopt);
+    i -= 1;
+    j -= 1;
+    if (i == 0) i = 97;
+    else if (j == 0) j = 97;
+    c -= 7654321;
+    if (c < 0) c += 16777213;
+    iopt -= c;
+    if (iopt < 0) iopt += 16777216;
+    return iopt;
+  }
+};
+
+// Same generator on a plain int array in global memory (state words at
+// u[k*stride]); used where a stream is drawn outside the transport kernels.
+struct RanmarGlobal {
+  int *u;
+  int stride;
+  int i, j, c;
   __device__ __forceinline__ int next_int() {
     int iopt = u[(i - 1) * stride] - u[(j - 1) * stride];
     if (iopt < 0) iopt += 16777216;

@@ -24,7 +24,15 @@ using omc::fail;
 
 namespace {
 
-constexpr int kBlock = 128;  // lanes per block; the RNG state of a block is 97*kBlock ints of shared memory
+constexpr int kBlock = 128;  // lanes per block
+// Shared memory of a block: the RANMAR states of its lanes, 3 bytes a word.
+constexpr size_t kRngSmem = static_cast<size_t>(RNG_WORDS) * kBlock * 3;
+// Blocks per SM the register budget is sized for: FP32 fits the 6 blocks
+// the shared memory allows; FP64 needs more registers.
+template <typename R>
+struct Occupancy {
+  static constexpr int kMinBlocks = sizeof(R) == 4 ? 6 : 3;
+};
 constexpr int kDefaultDepth = 48;
 
 #define CUDA_TRY(expr)                                                                           \
@@ -50,7 +58,7 @@ __global__ void seed_kernel(int ixx, int jxx, int nlanes, int *rng_u, int *rng_i
 __global__ void ranmar_draw_kernel(int nlanes, long long n, int *rng_u, int *rng_ijc, int *out) {
   int lane = blockIdx.x * blockDim.x + threadIdx.x;
   if (lane >= nlanes) return;
-  Ranmar r;
+  RanmarGlobal r;
   r.u = rng_u + lane;
   r.stride = nlanes;
   r.i = rng_ijc[lane];
@@ -62,14 +70,37 @@ __global__ void ranmar_draw_kernel(int nlanes, long long n, int *rng_u, int *rng
   rng_ijc[2 * nlanes + lane] = r.c;
 }
 
+// Shared-memory RANMAR planes of a block: [97][kBlock] low halves, then
+// [97][kBlock] high bytes.
+struct RngPlanes {
+  unsigned short *lo;
+  unsigned char *hi;
+};
+__device__ __forceinline__ RngPlanes rng_planes(unsigned char *smem) {
+  return RngPlanes{reinterpret_cast<unsigned short *>(smem), smem + static_cast<size_t>(RNG_WORDS) * kBlock * 2};
+}
+__device__ __forceinline__ void rng_to_smem(const int *g, int nlanes, int gl, RngPlanes s, int t) {
+  for (int k = 0; k < RNG_WORDS; k++) {
+    int v = g[static_cast<size_t>(k) * nlanes + gl];
+    s.lo[k * kBlock + t] = static_cast<unsigned short>(v & 0xffff);
+    s.hi[k * kBlock + t] = static_cast<unsigned char>(v >> 16);
+  }
+}
+__device__ __forceinline__ void rng_from_smem(int *g, int nlanes, int gl, RngPlanes s, int t) {
+  for (int k = 0; k < RNG_WORDS; k++)
+    g[static_cast<size_t>(k) * nlanes + gl] =
+        static_cast<int>(s.lo[k * kBlock + t]) | (static_cast<int>(s.hi[k * kBlock + t]) << 16);
+}
+
 template <typename R>
-__global__ void __launch_bounds__(kBlock) transport_kernel(Params<R> P) {
-  extern __shared__ int s_rng[];  // [97][kBlock]
+__global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) transport_kernel(Params<R> P) {
+  extern __shared__ unsigned char s_raw[];
   const int t = threadIdx.x;
   const int lane = blockIdx.x * kBlock + t;
   if (lane >= P.nlanes) return;
-  for (int k = 0; k < RNG_WORDS; k++) s_rng[k * kBlock + t] = P.rng_u[static_cast<size_t>(k) * P.nlanes + lane];
-  Lane<R, false> L(P, lane, s_rng + t, kBlock);
+  RngPlanes sp = rng_planes(s_raw);
+  rng_to_smem(P.rng_u, P.nlanes, lane, sp, t);
+  Lane<R, false> L(P, lane, sp.lo + t, sp.hi + t, kBlock);
   L.rng.i = P.rng_ijc[lane];
   L.rng.j = P.rng_ijc[P.nlanes + lane];
   L.rng.c = P.rng_ijc[2 * P.nlanes + lane];
@@ -90,7 +121,7 @@ __global__ void __launch_bounds__(kBlock) transport_kernel(Params<R> P) {
       L.np = -1;
     }
   }
-  for (int k = 0; k < RNG_WORDS; k++) P.rng_u[static_cast<size_t>(k) * P.nlanes + lane] = s_rng[k * kBlock + t];
+  rng_from_smem(P.rng_u, P.nlanes, lane, sp, t);
   P.rng_ijc[lane] = L.rng.i;
   P.rng_ijc[P.nlanes + lane] = L.rng.j;
   P.rng_ijc[2 * P.nlanes + lane] = L.rng.c;
@@ -165,13 +196,14 @@ __device__ bool grid_barrier(unsigned *arrive, unsigned *gen, unsigned nblocks) 
 __device__ __forceinline__ unsigned vload(const unsigned *p) { return *static_cast<const volatile unsigned *>(p); }
 
 template <typename R>
-__global__ void __launch_bounds__(kBlock) wavefront_kernel(Params<R> P, Wavefront<R> W) {
-  extern __shared__ int s_rng[];
+__global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) wavefront_kernel(Params<R> P, Wavefront<R> W) {
+  extern __shared__ unsigned char s_raw[];
   const int t = threadIdx.x;
   const int gtid = blockIdx.x * kBlock + t;
   const int lane_id = t & 31;
-  for (int k = 0; k < RNG_WORDS; k++) s_rng[k * kBlock + t] = P.rng_u[static_cast<size_t>(k) * P.nlanes + gtid];
-  Lane<R, true> L(P, gtid, s_rng + t, kBlock);
+  RngPlanes sp = rng_planes(s_raw);
+  rng_to_smem(P.rng_u, P.nlanes, gtid, sp, t);
+  Lane<R, true> L(P, gtid, sp.lo + t, sp.hi + t, kBlock);
   L.rng.i = P.rng_ijc[gtid];
   L.rng.j = P.rng_ijc[P.nlanes + gtid];
   L.rng.c = P.rng_ijc[2 * P.nlanes + gtid];
@@ -237,7 +269,7 @@ __global__ void __launch_bounds__(kBlock) wavefront_kernel(Params<R> P, Wavefron
     if (!grid_barrier(W.bar_arrive, W.bar_gen, gridDim.x)) L.err |= ERR_BARRIER;
   }
   if (it >= W.max_iters) L.err |= ERR_LOOP;
-  for (int k = 0; k < RNG_WORDS; k++) P.rng_u[static_cast<size_t>(k) * P.nlanes + gtid] = s_rng[k * kBlock + t];
+  rng_from_smem(P.rng_u, P.nlanes, gtid, sp, t);
   P.rng_ijc[gtid] = L.rng.i;
   P.rng_ijc[P.nlanes + gtid] = L.rng.j;
   P.rng_ijc[2 * P.nlanes + gtid] = L.rng.c;
@@ -300,6 +332,13 @@ struct DevArrays {
     cudaMemcpy(b.p, h.data(), n * sizeof(R), cudaMemcpyHostToDevice);
     bufs.push_back(b);
     return static_cast<const R *>(b.p);
+  }
+  const V4<R> *put4(const std::vector<V4<R>> &h) {
+    DevBuf b;
+    if (b.ensure((h.size() ? h.size() : 1) * sizeof(V4<R>)) != OMC_OK) return nullptr;
+    cudaMemcpy(b.p, h.data(), h.size() * sizeof(V4<R>), cudaMemcpyHostToDevice);
+    bufs.push_back(b);
+    return static_cast<const V4<R> *>(b.p);
   }
   const int *put_int(const int *src, size_t n) {
     DevBuf b;
@@ -445,6 +484,42 @@ omc_status upload_tables(PrecisionState<R> &S, const omc_tables *t) {
   T.ims = A.put_int(t->ims, nms);
   T.dllambi = static_cast<R>(t->dllambi);
   T.dqmsi = static_cast<R>(t->dqmsi);
+  // Packed interpolation records (layout in device.cuh).
+  auto v4 = [](double a, double b, double c, double d) {
+    return V4<R>{static_cast<R>(a), static_cast<R>(b), static_cast<R>(c), static_cast<R>(d)};
+  };
+  std::vector<V4<R>> pm(ng), pb(ng);
+  for (size_t i = 0; i < ng; i++) {
+    pm[i] = v4(t->gmfp1[i], t->gmfp0[i], t->cohe1[i], t->cohe0[i]);
+    pb[i] = v4(t->gbr11[i], t->gbr10[i], t->gbr21[i], t->gbr20[i]);
+  }
+  T.ph_mfp = A.put4(pm);
+  T.ph_br = A.put4(pb);
+  std::vector<V4<R>> sd(2 * ne), te(2 * ne), rg(2 * ne), qv(2 * ne), ib(ne), ib2(ne);
+  for (int q = 0; q < 2; q++)
+    for (size_t i = 0; i < ne; i++) {
+      size_t o = q * ne + i;
+      if (q == 0) {
+        sd[o] = v4(t->esig1[i], t->esig0[i], t->ededx1[i], t->ededx0[i]);
+        te[o] = v4(t->tmxs1[i], t->tmxs0[i], t->etae_ms1[i], t->etae_ms0[i]);
+        qv[o] = v4(t->q1ce_ms1[i], t->q1ce_ms0[i], t->q2ce_ms1[i], t->q2ce_ms0[i]);
+      } else {
+        sd[o] = v4(t->psig1[i], t->psig0[i], t->pdedx1[i], t->pdedx0[i]);
+        te[o] = v4(t->tmxs1[i], t->tmxs0[i], t->etap_ms1[i], t->etap_ms0[i]);
+        qv[o] = v4(t->q1cp_ms1[i], t->q1cp_ms0[i], t->q2cp_ms1[i], t->q2cp_ms0[i]);
+      }
+      rg[o] = v4(t->blcce1[i], t->blcce0[i], t->range_ep[o], t->e_array[i]);
+    }
+  for (size_t i = 0; i < ne; i++) {
+    ib[i] = v4(t->ebr11[i], t->ebr10[i], t->pbr11[i], t->pbr10[i]);
+    ib2[i] = v4(t->pbr21[i], t->pbr20[i], 0.0, 0.0);
+  }
+  T.el_sd = A.put4(sd);
+  T.el_te = A.put4(te);
+  T.el_rg = A.put4(rg);
+  T.el_q = A.put4(qv);
+  T.el_ib = A.put4(ib);
+  T.el_ib2 = A.put4(ib2);
   for (auto &b : A.bufs)
     if (!b.p) return fail(OMC_ERR_NOMEM, "table upload failed");
   cudaError_t e = cudaGetLastError();
@@ -529,7 +604,7 @@ omc_status run_batches(omc_engine *e, PrecisionState<R> &S, const omc_run_config
   P.n_dep = &dc->n_dep;
   P.max_np = &dc->max_np;
   P.err = &dc->err;
-  size_t smem = static_cast<size_t>(RNG_WORDS) * kBlock * sizeof(int);
+  size_t smem = kRngSmem;
   cudaFuncSetAttribute(transport_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
   int blocks = (nlanes + kBlock - 1) / kBlock;
   cudaEvent_t t0, t1;
@@ -581,7 +656,7 @@ struct WfCounters {
 
 template <typename R>
 int wavefront_blocks(omc_engine *e) {
-  size_t smem = static_cast<size_t>(RNG_WORDS) * kBlock * sizeof(int);
+  size_t smem = kRngSmem;
   cudaFuncSetAttribute(wavefront_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wavefront_kernel<R>, kBlock, smem);
@@ -594,7 +669,7 @@ omc_status run_wavefront(omc_engine *e, PrecisionState<R> &S, const omc_run_conf
   const int nsplit = cfg->nsplit < 1 ? 1 : cfg->nsplit;
   const int blocks = nlanes / kBlock;
   unsigned long long target = cfg->inflight > 0 ? static_cast<unsigned long long>(cfg->inflight)
-                                                 : static_cast<unsigned long long>(nlanes) * 8;
+                                                 : static_cast<unsigned long long>(nlanes) * 16;
   // Worst case growth in one iteration: every photon of a cycle leaves up
   // to two particles per split, every electron step up to two.
   unsigned long long cap = target * (4ull + 2ull * nsplit) + 4ull * nlanes;
@@ -644,7 +719,7 @@ omc_status run_wavefront(omc_engine *e, PrecisionState<R> &S, const omc_run_conf
   P.n_dep = &dc->n_dep;
   P.max_np = &dc->max_np;
   P.err = &dc->err;
-  size_t smem = static_cast<size_t>(RNG_WORDS) * kBlock * sizeof(int);
+  size_t smem = kRngSmem;
   cudaEvent_t t0, t1;
   cudaEventCreate(&t0);
   cudaEventCreate(&t1);
@@ -698,7 +773,7 @@ omc_status ensure_device(omc_engine *e) {
 template <typename R>
 int default_lanes(omc_engine *e) {
   int per_sm = 0;
-  size_t smem = static_cast<size_t>(RNG_WORDS) * kBlock * sizeof(int);
+  size_t smem = kRngSmem;
   cudaFuncSetAttribute(transport_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, transport_kernel<R>, kBlock, smem);
   if (per_sm < 1) per_sm = 1;

@@ -28,6 +28,16 @@ __device__ __forceinline__ R pwlf(const R *c1, const R *c0, int idx, R lv) {
   return lv * __ldg(c1 + idx) + __ldg(c0 + idx);
 }
 
+__device__ __forceinline__ V4<float> ld4(const V4<float> *p) {
+  float4 v = __ldg(reinterpret_cast<const float4 *>(p));
+  return V4<float>{v.x, v.y, v.z, v.w};
+}
+__device__ __forceinline__ V4<double> ld4(const V4<double> *p) {
+  const double2 *q = reinterpret_cast<const double2 *>(p);
+  double2 a = __ldg(q), b = __ldg(q + 1);
+  return V4<double>{a.x, a.y, b.x, b.y};
+}
+
 // Output queues of the current wavefront phase.
 template <typename R>
 struct EmitTargets {
@@ -62,8 +72,10 @@ struct Lane {
   unsigned long long n_geom;  // howfar calls (voxel-stepping decisions)
   unsigned long long n_dep;   // ausgab calls (energy deposits)
 
-  __device__ Lane(const Params<R> &prm, int ln, int *su, int sstride) : P(prm), lane(ln) {
-    rng.u = su;
+  __device__ Lane(const Params<R> &prm, int ln, unsigned short *slo, unsigned char *shi, int sstride)
+      : P(prm), lane(ln) {
+    rng.lo = slo;
+    rng.hi = shi;
     rng.stride = sstride;
     np = -1;
     ensrc = 0.0;
@@ -266,6 +278,15 @@ struct Lane {
     t = fmin(t, q.z - __ldg(g.zb + irz));
     return t;
   }
+
+  // ---- packed interpolation records ---------------------------------------
+  __device__ __forceinline__ size_t eidx(int qel, int m, int l) const {
+    return (static_cast<size_t>(qel) * P.T.nmed + m) * MXEKE + l;
+  }
+  __device__ __forceinline__ V4<R> esd(int qel, int m, int l) const { return ld4(P.T.el_sd + eidx(qel, m, l)); }
+  __device__ __forceinline__ V4<R> ete(int qel, int m, int l) const { return ld4(P.T.el_te + eidx(qel, m, l)); }
+  __device__ __forceinline__ V4<R> erg(int qel, int m, int l) const { return ld4(P.T.el_rg + eidx(qel, m, l)); }
+  __device__ __forceinline__ V4<R> eq(int qel, int m, int l) const { return ld4(P.T.el_q + eidx(qel, m, l)); }
 
   // ---- interpolation indices, clamped to the table --------------------------
   __device__ __forceinline__ int photon_bin(int imed, R gle) {
