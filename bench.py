@@ -125,7 +125,7 @@ def profiled_traffic():
     """DRAM bytes per history of the transport kernel from the committed
     ncu summary (profiles/), or None."""
     try:
-        with open(os.path.join(ROOT, "profiles", "transport_fp32_slab150.json")) as f:
+        with open(os.path.join(ROOT, "profiles", "wavefront_fp32_slab150.json")) as f:
             return float(json.load(f)["dram_bytes_per_history"])
     except (OSError, KeyError, ValueError):
         return None
@@ -234,7 +234,7 @@ def run_ours(args, rank, world, local_rank, dist_on):
             evs += st.steps
             acc += a
             acc2 += a * a
-            launches += 2  # transport, batch accumulation (streams continue: no seeding)
+            launches += 2  # wavefront transport, batch accumulation (streams continue: no seeding)
         barrier()
         clocks = sampler.stop()
         dev_ms = float(sum(step_ms))
@@ -303,7 +303,7 @@ def run_ours(args, rank, world, local_rank, dist_on):
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "peak_kind": peak_kind,
                              "traffic": (traffic_ph * H) if traffic_ph else None,
-                             "kernel": "transport_kernel<float>",
+                             "kernel": "wavefront_kernel<float>",
                              "atomics_per_s": dep / (dev_ms / 1000.0)},
                 "cpu_baseline": cpu,
                 "e2e": {"value": e2e_value, "unit": "histories/s", "h2d_bytes_per_step": int(h2d),

@@ -669,7 +669,7 @@ omc_status run_wavefront(omc_engine *e, PrecisionState<R> &S, const omc_run_conf
   const int nsplit = cfg->nsplit < 1 ? 1 : cfg->nsplit;
   const int blocks = nlanes / kBlock;
   unsigned long long target = cfg->inflight > 0 ? static_cast<unsigned long long>(cfg->inflight)
-                                                 : static_cast<unsigned long long>(nlanes) * 16;
+                                                 : static_cast<unsigned long long>(nlanes) * 32;
   // Worst case growth in one iteration: every photon of a cycle leaves up
   // to two particles per split, every electron step up to two.
   unsigned long long cap = target * (4ull + 2ull * nsplit) + 4ull * nlanes;
