@@ -60,7 +60,7 @@ def test_many_lanes_statistically_identical(name, ncase, precision, schedule, en
     """Per-voxel z-scores of the GPU against the OpenMP-seeded oracle over
     voxels above 20% of Dmax (50 batches): the count outside 2 sigma and
     the sum of z^2 are what two samples of one distribution give, and the
-    total energy agrees within 1%."""
+    total energies agree within 6/sqrt(N)."""
     prob = problem_factory(name, ncase=ncase, nbatch=50, seeds=(33, 97))
     engine.load(prob)
     g, g2, st = engine.run(precision=precision, schedule=schedule)
@@ -69,11 +69,14 @@ def test_many_lanes_statistically_identical(name, ncase, precision, schedule, en
     c = compare(g, g2, o, o2, prob.nbatch)
     assert c["n"] >= 10, c
     assert consistent(c), c
-    assert abs(c["etot_rel"]) < 0.01, c
+    # The total deposit of N histories scatters by roughly 1/sqrt(N).
+    assert abs(c["etot_rel"]) < 6.0 / np.sqrt(ncase), c
     if prob.source.contents.spectrum == 0:
         assert st.ensrc == pytest.approx(res.ensrc, rel=1e-12)
     else:
-        assert st.ensrc == pytest.approx(res.ensrc, rel=0.01)
+        # Sampled spectrum energies: the relative spread of a single energy is
+        # below 1, so two sums of N agree within 4/sqrt(N) at 4 sigma or more.
+        assert st.ensrc == pytest.approx(res.ensrc, rel=4.0 / np.sqrt(ncase))
 
 
 def test_fp32_against_fp64_on_the_gpu(engine, problem_factory):
