@@ -92,7 +92,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
     cli = os.path.join(CSRC, "frontend", "omc_dosxyz.c")
     if os.path.exists(cli) and (force or _stale(BIN, [cli, LIB, os.path.join(INCLUDE, "omc_gpu.h")])):
         subprocess.run(["gcc", "-O2", "-std=gnu11", f"-I{INCLUDE}", cli, "-o", BIN, f"-L{os.path.dirname(LIB)}",
-                        "-lompmc_gb300", f"-Wl,-rpath,{os.path.dirname(LIB)}", "-lm"], check=True)
+                        "-lompmc_gb300", "-Wl,-rpath,$ORIGIN/../../lib/" + MACHINE, "-lm"], check=True)
     return LIB
 
 
