@@ -114,6 +114,7 @@ def lib(path: str | None = None):
         "omc_engine_set_source": ([vp, pp(Source_t)], C.c_int),
         "omc_engine_run": ([vp, pp(RunConfig_t), pp(C.c_double), pp(C.c_double), pp(RunStats_t)], C.c_int),
         "omc_engine_run_resident": ([vp, pp(RunConfig_t), pp(vp), pp(vp), pp(RunStats_t)], C.c_int),
+        "omc_engine_run_noalloc": ([vp, pp(RunConfig_t), C.c_void_p, pp(RunStats_t)], C.c_int),
         "omc_gpu_ranmar": ([C.c_int, C.c_int, C.c_int, C.c_int, C.c_longlong, pp(C.c_int32)], C.c_int),
         "omc_stream_seeds": ([C.c_int, C.c_int, C.c_longlong, pp(C.c_int), pp(C.c_int)], None),
     }

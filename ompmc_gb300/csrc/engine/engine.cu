@@ -966,3 +966,138 @@ extern "C" omc_status omc_gpu_ranmar(int device, int ixx, int jxx, int nstreams,
   if (err != cudaSuccess) return fail(OMC_ERR_CUDA, "ranmar: %s", cudaGetErrorString(err));
   return OMC_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Transport without device allocation (omc_engine_run_noalloc).  The
+// per-lane transport kernel runs on scratch taken from one file-scope
+// device array instead of engine buffers, and deposits into the caller's
+// device tally.  Layout of the array (byte offsets, sized for FP64):
+//   RANMAR words   [97][OMC_NOALLOC_MAX_LANES] int
+//   RANMAR i/j/c   [3][OMC_NOALLOC_MAX_LANES] int
+//   stack planes   [8][OMC_NOALLOC_MAX_DEPTH][OMC_NOALLOC_MAX_LANES] double
+//   stack keys     [OMC_NOALLOC_MAX_DEPTH][OMC_NOALLOC_MAX_LANES] int
+//   counters       256 bytes
+// ---------------------------------------------------------------------------
+#include <chrono>
+#include <mutex>
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[OMC_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+
+constexpr int kNoallocMaxDevices = 64;
+constexpr size_t kNoallocRngBytes = static_cast<size_t>(OMC_NOALLOC_MAX_LANES) * 97 * 4;
+constexpr size_t kNoallocIjcBytes = static_cast<size_t>(OMC_NOALLOC_MAX_LANES) * 3 * 4;
+constexpr size_t kNoallocStackBytes = static_cast<size_t>(OMC_NOALLOC_MAX_LANES) * OMC_NOALLOC_MAX_DEPTH * 8 * 8;
+constexpr size_t kNoallocKeyBytes = static_cast<size_t>(OMC_NOALLOC_MAX_LANES) * OMC_NOALLOC_MAX_DEPTH * 4;
+static_assert(kNoallocRngBytes + kNoallocIjcBytes + kNoallocStackBytes + kNoallocKeyBytes + 256 ==
+                  OMC_NOALLOC_SCRATCH_BYTES,
+              "scratch layout and OMC_NOALLOC_SCRATCH_BYTES disagree");
+static_assert(sizeof(Counters) <= 256, "counters do not fit their scratch slot");
+
+std::mutex g_noalloc_mu;
+unsigned char *g_noalloc_ptr[kNoallocMaxDevices] = {};
+int g_noalloc_lanes[kNoallocMaxDevices] = {};  // lane count the streams in the array were seeded for
+
+// Device address of the scratch array on `device`, looked up once per
+// device with that device current.  The host-side symbol is only a
+// stand-in and must never be passed to a kernel.
+omc_status noalloc_scratch(int device, unsigned char **out) {
+  if (device < 0 || device >= kNoallocMaxDevices) return fail(OMC_ERR_ARG, "device %d unsupported", device);
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[device]) {
+    void *p = nullptr;
+    cudaError_t err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (err != cudaSuccess || !p)
+      return fail(OMC_ERR_CUDA, "cudaGetSymbolAddress(scratch) on device %d: %s", device, cudaGetErrorString(err));
+    g_noalloc_ptr[device] = static_cast<unsigned char *>(p);
+  }
+  *out = g_noalloc_ptr[device];
+  return OMC_OK;
+}
+
+template <typename R>
+omc_status run_noalloc(omc_engine *e, PrecisionState<R> &S, const omc_run_config *cfg, int nlanes, int depth,
+                       double *d_endep, omc_run_stats *stats) {
+  unsigned char *base = nullptr;
+  omc_status s = noalloc_scratch(e->device, &base);
+  if (s != OMC_OK) return s;
+  int *rng_u = reinterpret_cast<int *>(base);
+  int *rng_ijc = reinterpret_cast<int *>(base + kNoallocRngBytes);
+  R *stk = reinterpret_cast<R *>(base + kNoallocRngBytes + kNoallocIjcBytes);
+  int *keys = reinterpret_cast<int *>(base + kNoallocRngBytes + kNoallocIjcBytes + kNoallocStackBytes);
+  Counters *dc = reinterpret_cast<Counters *>(base + kNoallocRngBytes + kNoallocIjcBytes + kNoallocStackBytes +
+                                              kNoallocKeyBytes);
+  auto t0 = std::chrono::steady_clock::now();
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!(cfg->continue_streams && g_noalloc_lanes[e->device] == nlanes)) {
+      seed_kernel<<<(nlanes + 255) / 256, 256, 0, e->stream>>>(cfg->ixx, cfg->jxx, nlanes, rng_u, rng_ijc);
+      g_noalloc_lanes[e->device] = nlanes;
+    }
+  }
+  cudaMemsetAsync(dc, 0, sizeof(Counters), e->stream);  // counters must start at zero
+  Params<R> P{};
+  P.T = S.T;
+  P.G = S.G;
+  P.S = S.S;
+  P.nsplit = cfg->nsplit < 1 ? 1 : cfg->nsplit;
+  P.nlanes = nlanes;
+  P.depth = depth;
+  P.nhist = cfg->nperbatch;
+  P.next = &dc->next;
+  P.rng_u = rng_u;
+  P.rng_ijc = rng_ijc;
+  P.stk = stk;
+  P.stk_key = keys;
+  P.endep = d_endep;
+  P.ensrc = &dc->ensrc;
+  P.events = &dc->events;
+  P.n_geom = &dc->n_geom;
+  P.n_dep = &dc->n_dep;
+  P.max_np = &dc->max_np;
+  P.err = &dc->err;
+  transport_kernel<R><<<(nlanes + kBlock - 1) / kBlock, kBlock, kRngSmem, e->stream>>>(P);
+  cudaError_t err = cudaGetLastError();
+  if (err == cudaSuccess) err = cudaStreamSynchronize(e->stream);
+  if (err != cudaSuccess) return fail(OMC_ERR_CUDA, "no-alloc transport: %s", cudaGetErrorString(err));
+  Counters hc{};
+  err = cudaMemcpy(&hc, dc, sizeof hc, cudaMemcpyDeviceToHost);
+  if (err != cudaSuccess) return fail(OMC_ERR_CUDA, "no-alloc counters: %s", cudaGetErrorString(err));
+  double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  if (stats) {
+    stats->ensrc = hc.ensrc;
+    stats->transport_ms = ms;
+    stats->kernel_ms = ms;
+    stats->histories = cfg->nperbatch;
+    stats->steps = static_cast<long long>(hc.events);
+    stats->voxel_steps = static_cast<long long>(hc.n_geom);
+    stats->deposits = static_cast<long long>(hc.n_dep);
+    stats->max_stack = hc.max_np + 1;
+    stats->error_flags = static_cast<int>(hc.err);
+  }
+  if (hc.err & ERR_STACK) return fail(OMC_ERR_STACK, "particle stack overflow (depth %d); histories were dropped", depth);
+  if (hc.err & (ERR_LOOP | ERR_EVENTS)) return fail(OMC_ERR_LIMIT, "a device loop hit its iteration limit");
+  return OMC_OK;
+}
+
+}  // namespace
+
+extern "C" omc_status omc_engine_run_noalloc(omc_engine *e, const omc_run_config *cfg, double *d_endep,
+                                             omc_run_stats *stats) {
+  if (!e || !cfg || !d_endep) return fail(OMC_ERR_ARG, "null argument");
+  if (!e->f64.tables_ok || !e->f64.geom_ok || !e->f64.source_ok)
+    return fail(OMC_ERR_STATE, "tables, geometry and source must be set before a run");
+  if (cfg->nbatch != 1) return fail(OMC_ERR_ARG, "omc_engine_run_noalloc transports one batch per call (nbatch = 1)");
+  if (cfg->nperbatch < 0) return fail(OMC_ERR_ARG, "nperbatch must be >= 0");
+  if (cfg->precision != OMC_FP64 && cfg->precision != OMC_FP32) return fail(OMC_ERR_ARG, "unknown precision");
+  int nlanes = cfg->serial ? 1 : (cfg->nlanes > 0 ? cfg->nlanes : OMC_NOALLOC_MAX_LANES);
+  if (nlanes > OMC_NOALLOC_MAX_LANES)
+    return fail(OMC_ERR_ARG, "nlanes %d exceeds the no-allocation maximum of %d lanes", nlanes, OMC_NOALLOC_MAX_LANES);
+  int depth = cfg->stack_depth > 0 ? cfg->stack_depth : OMC_NOALLOC_MAX_DEPTH;
+  if (depth > OMC_NOALLOC_MAX_DEPTH)
+    return fail(OMC_ERR_ARG, "stack depth %d exceeds the no-allocation maximum of %d", depth, OMC_NOALLOC_MAX_DEPTH);
+  if (cudaSetDevice(e->device) != cudaSuccess) return fail(OMC_ERR_CUDA, "cudaSetDevice(%d) failed", e->device);
+  if (cfg->precision == OMC_FP64) return run_noalloc(e, e->f64, cfg, nlanes, depth, d_endep, stats);
+  return run_noalloc(e, e->f32, cfg, nlanes, depth, d_endep, stats);
+}
