@@ -350,6 +350,73 @@ omc_status omc_gpu_ranmar(int device, int ixx, int jxx, int nstreams,
 /* Seed pair of stream k under the rule above (host helper). */
 void omc_stream_seeds(int ixx, int jxx, long long k, int *ixx_k, int *jxx_k);
 
+/* ------------------------------------------------------------------------
+ * Dose-influence matrix (omc_matrad).  Replaces the beamlet loop of the
+ * matRad front end (ucodes/omc_matrad/omc_matrad.c:1374-1512): for every
+ * beamlet, its histories start on the beamlet's bixel, its dose is
+ * accumulated separately, converted to Gy per history, thresholded at
+ * rel_threshold x the beamlet's maximum and stored as one column of a
+ * compressed-sparse-column matrix over voxels x beamlets (equivalently CSR
+ * over beamlets x voxels).
+ * ---------------------------------------------------------------------- */
+
+/* Beamlet geometry, the fields of matRad's mcSrc structure
+ * (omc_matrad.c:543-750): every beamlet is a parallelogram at the
+ * isocentre plane, corner + a*side1 + b*side2 with a, b uniform in [0,1),
+ * irradiated from the source point of its beam.  All coordinates in cm in
+ * the phantom frame. */
+typedef struct omc_beamlets {
+    int nbeamlets;               /* mcSrc.nBixels                          */
+    int nbeams;                  /* entries of the source-point arrays     */
+    const int *ibeam;            /* [nbeamlets] beam, 0-based (iBeam - 1)  */
+    const double *xsource, *ysource, *zsource; /* [nbeams]                 */
+    const double *xcorner, *ycorner, *zcorner; /* [nbeamlets]              */
+    const double *xside1, *yside1, *zside1;    /* [nbeamlets]              */
+    const double *xside2, *yside2, *zside2;    /* [nbeamlets]              */
+} omc_beamlets;
+
+/* Uploads the beamlets; the energy spectrum (or mono energy) and charge
+ * still come from omc_engine_set_source.  Requires the geometry. */
+omc_status omc_engine_set_beamlets(omc_engine *e, const omc_beamlets *b);
+
+typedef struct omc_dij {
+    int nrows;           /* voxels, nx*ny*nz (row = region index - 1)      */
+    int ncols;           /* beamlets                                       */
+    long long nnz;       /* stored entries                                 */
+    long long *col_ptr;  /* [ncols+1] (mxGetJc)                            */
+    int *row_idx;        /* [nnz], ascending within a column (mxGetIr)     */
+    double *values;      /* [nnz] (mxGetPr); NULL when fp32_values was set */
+    float *values_f32;   /* [nnz] when fp32_values was set, else NULL      */
+} omc_dij;
+
+void omc_dij_free(omc_dij *d);
+
+typedef struct omc_dij_config {
+    double rel_threshold;   /* "relative dose threshold": keep entries
+                               strictly above this x the column maximum   */
+    const long long *nhist; /* [nbeamlets] histories of each beamlet, or
+                               NULL: cfg->nperbatch * cfg->nbatch each
+                               (the reference's uniform count)             */
+    int fp32_values;        /* 1 = store FP32 values (FP64 accumulation)  */
+    long long tally_bytes;  /* device memory for the beamlet tallies that
+                               are transported together; 0 = automatic     */
+} omc_dij_config;
+
+/* Transports every beamlet's histories and returns the dij in *out (free
+ * with omc_dij_free).  Values follow the reference: (sum of the beamlet's
+ * energy deposits / nbatch) x 1.602e-10 / (voxel mass x histories of the
+ * beamlet), zero where the voxel density is below 0.044 g/cm^3
+ * (omc_matrad.c:839-919; the division by nbatch comes from the reference
+ * passing the total history count, omc_matrad.c:1418).  cfg->nbatch only
+ * enters that normalisation.  With cfg->serial = 1 the beamlets run one
+ * after another on one RANMAR stream in the reference's serial order.
+ * Beamlets otherwise share one launch: as many beamlet tallies as fit in
+ * tally_bytes are resident at once, and histories of different beamlets
+ * are in flight together. */
+omc_status omc_engine_run_dij(omc_engine *e, const omc_run_config *cfg,
+                              const omc_dij_config *dcfg, omc_dij **out,
+                              omc_run_stats *stats);
+
 #ifdef __cplusplus
 }
 #endif

@@ -71,6 +71,23 @@ class RunStats_t(C.Structure):
                 ("voxel_steps", C.c_longlong), ("deposits", C.c_longlong), ("kernel_ms", C.c_double)]
 
 
+class Beamlets_t(C.Structure):
+    _fields_ = [("nbeamlets", C.c_int), ("nbeams", C.c_int), ("ibeam", C.POINTER(C.c_int))] + [
+        (n, C.POINTER(C.c_double)) for n in ("xsource", "ysource", "zsource", "xcorner", "ycorner", "zcorner",
+                                             "xside1", "yside1", "zside1", "xside2", "yside2", "zside2")]
+
+
+class Dij_t(C.Structure):
+    _fields_ = [("nrows", C.c_int), ("ncols", C.c_int), ("nnz", C.c_longlong),
+                ("col_ptr", C.POINTER(C.c_longlong)), ("row_idx", C.POINTER(C.c_int)),
+                ("values", C.POINTER(C.c_double)), ("values_f32", C.POINTER(C.c_float))]
+
+
+class DijConfig_t(C.Structure):
+    _fields_ = [("rel_threshold", C.c_double), ("nhist", C.POINTER(C.c_longlong)), ("fp32_values", C.c_int),
+                ("tally_bytes", C.c_longlong)]
+
+
 _lib = None
 
 
@@ -115,6 +132,9 @@ def lib(path: str | None = None):
         "omc_engine_run": ([vp, pp(RunConfig_t), pp(C.c_double), pp(C.c_double), pp(RunStats_t)], C.c_int),
         "omc_engine_run_resident": ([vp, pp(RunConfig_t), pp(vp), pp(vp), pp(RunStats_t)], C.c_int),
         "omc_engine_run_noalloc": ([vp, pp(RunConfig_t), C.c_void_p, pp(RunStats_t)], C.c_int),
+        "omc_engine_set_beamlets": ([vp, pp(Beamlets_t)], C.c_int),
+        "omc_engine_run_dij": ([vp, pp(RunConfig_t), pp(DijConfig_t), pp(pp(Dij_t)), pp(RunStats_t)], C.c_int),
+        "omc_dij_free": ([pp(Dij_t)], None),
         "omc_gpu_ranmar": ([C.c_int, C.c_int, C.c_int, C.c_int, C.c_longlong, pp(C.c_int32)], C.c_int),
         "omc_stream_seeds": ([C.c_int, C.c_int, C.c_longlong, pp(C.c_int), pp(C.c_int)], None),
     }

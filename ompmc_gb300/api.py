@@ -218,6 +218,54 @@ class Engine:
         check(N.lib().omc_engine_run_resident(self._h, C.byref(cfg), C.byref(d1), C.byref(d2), C.byref(st)))
         return d1.value, d2.value, st
 
+    def set_beamlets(self, beamlets):
+        """Upload a :class:`ompmc_gb300.workloads.Beamlets` set (the
+        matRad mcSrc fields)."""
+        b = beamlets
+        keep = [np.ascontiguousarray(b.ibeam, dtype=np.int32)]
+        cols = []
+        for arr in (b.source[:, 0], b.source[:, 1], b.source[:, 2], b.corner[:, 0], b.corner[:, 1], b.corner[:, 2],
+                    b.side1[:, 0], b.side1[:, 1], b.side1[:, 2], b.side2[:, 0], b.side2[:, 1], b.side2[:, 2]):
+            a = np.ascontiguousarray(arr, dtype=np.float64)
+            keep.append(a)
+            cols.append(_dptr(a))
+        st = N.Beamlets_t(len(b.ibeam), len(b.source), keep[0].ctypes.data_as(C.POINTER(C.c_int)), *cols)
+        check(N.lib().omc_engine_set_beamlets(self._h, C.byref(st)))
+        self._beamlets = b
+        return self
+
+    def run_dij(self, rel_threshold=1e-4, nhist=None, nperbatch=None, nbatch=None, seeds=None, nsplit=None,
+                precision=FP64, serial=0, schedule=AUTO, fp32_values=False, tally_bytes=0, nlanes=0,
+                continue_streams=0):
+        """Dose-influence matrix of the uploaded beamlets; returns
+        (col_ptr, row_idx, values, stats) with values per history
+        (omc_engine_run_dij)."""
+        p = self._problem
+        cfg = self.config(p.nperbatch if nperbatch is None else nperbatch, p.nbatch if nbatch is None else nbatch,
+                          p.seeds if seeds is None else seeds, p.nsplit if nsplit is None else nsplit,
+                          precision, nlanes, 0, serial, continue_streams, schedule, 0)
+        nh = None
+        if nhist is not None:
+            nh = np.ascontiguousarray(nhist, dtype=np.int64)
+        dc = N.DijConfig_t(float(rel_threshold), nh.ctypes.data_as(C.POINTER(C.c_longlong)) if nh is not None
+                           else None, 1 if fp32_values else 0, int(tally_bytes))
+        out = C.POINTER(N.Dij_t)()
+        st = N.RunStats_t()
+        check(N.lib().omc_engine_run_dij(self._h, C.byref(cfg), C.byref(dc), C.byref(out), C.byref(st)))
+        try:
+            d = out.contents
+            col_ptr = np.ctypeslib.as_array(d.col_ptr, shape=(d.ncols + 1,)).copy()
+            if d.nnz:
+                rows = np.ctypeslib.as_array(d.row_idx, shape=(d.nnz,)).copy()
+                vp = d.values_f32 if fp32_values else d.values
+                vals = np.ctypeslib.as_array(vp, shape=(d.nnz,)).copy()
+            else:
+                rows = np.zeros(0, np.int32)
+                vals = np.zeros(0, np.float32 if fp32_values else np.float64)
+        finally:
+            N.lib().omc_dij_free(out)
+        return col_ptr, rows, vals, st
+
     def close(self):
         if getattr(self, "_h", None):
             N.lib().omc_engine_destroy(self._h)

@@ -104,7 +104,9 @@ struct Geometry {
   const R *ecut_m, *pcut_m;  // per medium (+1 slot for vacuum at index 0)
 };
 
-// Source (initSource, omc_dosxyz.c:368-632) in R.
+// Source (initSource, omc_dosxyz.c:368-632) in R.  With beamlets set
+// (omc_matrad.c:543-750) histories start on a beamlet's bixel instead of
+// the collimated point source.
 template <typename R>
 struct Source {
   int spectrum, charge;
@@ -112,6 +114,10 @@ struct Source {
   const R *cdfinv1, *cdfinv2;  // [INVDIM]
   R ssd, xinl, yinl, xsize, ysize;
   int ixinl, iyinl;
+  int beamlets;        // 1: beamlet source
+  const R *bixel;      // [nbeamlets][9] corner xyz, side1 xyz, side2 xyz
+  const R *beam_src;   // [nbeams][3] source point of each beam
+  const int *ibeam;    // [nbeamlets]
 };
 
 template <typename R>
@@ -129,8 +135,15 @@ struct Params {
   int *rng_ijc;              // [3][nlanes]
   R *stk;                    // [8][depth][nlanes]
   int *stk_key;              // [depth][nlanes]  ir*4 + iq+1
+  // beamlet jobs: history h of the launch belongs to tally slot s with
+  // slot_first[s] <= h < slot_first[s+1]; slot s scores into
+  // endep[s*nreg ...] and transports beamlet slot_beamlet[s]
+  int nslots;                        // 0: one tally, no beamlets
+  const long long *slot_first;       // [nslots+1]
+  const int *slot_beamlet;           // [nslots]
+  long long tally_stride;            // nreg
   // outputs
-  double *endep;             // [nreg] batch tally
+  double *endep;             // [nreg] batch tally ([nslots][nreg] with slots)
   double *ensrc;             // [1]
   unsigned long long *events;
   unsigned long long *n_geom;

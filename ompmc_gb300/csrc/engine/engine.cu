@@ -12,6 +12,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -110,7 +111,7 @@ __global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) transport_ke
     if (L.np < 0) {
       unsigned long long h = atomicAdd(P.next, 1ull);
       if (h >= static_cast<unsigned long long>(P.nhist)) break;
-      L.init_history();
+      L.init_history(static_cast<long long>(h));
       hist_events = 0;
     }
     if (L.p.iq == 0) L.photon_event();
@@ -148,6 +149,7 @@ struct Wavefront {
   int *ph_k[2];
   R *el_f[2];
   int *el_k[2];
+  int *ph_s[2], *el_s[2]; // tally slot per queued particle (beamlet jobs), else null
   unsigned cap;           // slots per queue
   unsigned *ctr;          // [0..2] photon counters, [3..5] electron counters
   unsigned long long *work;      // [3] chunk counters of the phase
@@ -233,7 +235,8 @@ __global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) wavefront_ke
     // One phase: new histories, then photons, then electrons, each range
     // padded to a multiple of 32 so that a warp's chunk is one code path.
     // Everything produced goes to the next iteration's queues.
-    L.out = EmitTargets<R>{W.ph_f[bout], W.ph_k[bout], W.ctr + cout, W.el_f[bout], W.el_k[bout], W.ctr + 3 + cout};
+    L.out = EmitTargets<R>{W.ph_f[bout], W.ph_k[bout], W.ctr + cout, W.el_f[bout], W.el_k[bout], W.ctr + 3 + cout,
+                           W.ph_s[bout], W.el_s[bout]};
     const unsigned long long m_pad = (static_cast<unsigned long long>(m) + 31) & ~31ull;
     const unsigned long long ph_pad = (static_cast<unsigned long long>(n_ph) + 31) & ~31ull;
     const unsigned long long total = m_pad + ph_pad + n_el;
@@ -245,13 +248,13 @@ __global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) wavefront_ke
       const unsigned long long i = base + lane_id;
       if (base < m_pad) {
         if (i < static_cast<unsigned long long>(m)) {
-          L.init_history();
+          L.init_history(static_cast<long long>(injected + i));
           L.emit(L.p);
         }
       } else if (base < m_pad + ph_pad) {
         const unsigned long long k = i - m_pad;
         if (k < n_ph) {
-          L.take(W.ph_f[bin], W.ph_k[bin], static_cast<unsigned>(k));
+          L.take(W.ph_f[bin], W.ph_k[bin], static_cast<unsigned>(k), W.ph_s[bin]);
           L.wf_photon_event();
           events++;
         }
@@ -259,7 +262,7 @@ __global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) wavefront_ke
         const unsigned long long k = i - m_pad - ph_pad;
         if (k < n_el) {
           // One step: one iteration of electron()'s tstep loop.
-          L.take(W.el_f[bin], W.el_k[bin], static_cast<unsigned>(k));
+          L.take(W.el_f[bin], W.el_k[bin], static_cast<unsigned>(k), W.el_s[bin]);
           L.electron_event();
           if (L.alive) L.emit(L.p);
           events++;
@@ -290,6 +293,153 @@ __global__ void accumulate_kernel(double *endep, double *acc, double *acc2, long
     acc[i] += e;
     acc2[i] += e * e;
     endep[i] = 0.0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Dose-influence matrix (omc_matrad.c:839-919 and :1426-1482), one tally
+// slot per beamlet: dose in place, slot maximum, then threshold and an
+// order-preserving compaction into CSC columns.  Tiles of kDijTile voxels
+// are counted, the counts scanned, and each tile written in 16 coalesced
+// rounds of 256 voxels.
+// ---------------------------------------------------------------------------
+constexpr int kDijThreads = 256;
+constexpr int kDijRounds = 16;
+constexpr int kDijTile = kDijThreads * kDijRounds;
+
+__device__ __forceinline__ double block_max(double v, double *red) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  }
+  return v;
+}
+
+// Energy to Gy per history, in the reference's operation order:
+// (sum / nbatch) * (1.602e-10 / (dx*dy*dz*rho * nhist)); zero below
+// 0.044 g/cm^3.  Grid: x over voxels, y over slots.
+__global__ void dij_dose_kernel(double *tally, long long nreg, int nx, int ny, const double *xb, const double *yb,
+                                const double *zb, const double *density, const double *slot_nhist, int nbatch,
+                                unsigned long long *slot_max) {
+  __shared__ double red[32];
+  const int s = blockIdx.y;
+  double *t = tally + static_cast<size_t>(s) * nreg + 1;
+  const double nh = slot_nhist[s];
+  const long long nvox = nreg - 1;
+  double m = 0.0;
+  for (long long v = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; v < nvox;
+       v += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int ix = static_cast<int>(v % nx);
+    const long long r = v / nx;
+    const int iy = static_cast<int>(r % ny);
+    const int iz = static_cast<int>(r / ny);
+    double endep = __ddiv_rn(t[v], static_cast<double>(nbatch));
+    double mass = __dmul_rn(__dmul_rn(__dsub_rn(xb[ix + 1], xb[ix]), __dsub_rn(yb[iy + 1], yb[iy])),
+                            __dsub_rn(zb[iz + 1], zb[iz]));
+    const double rho = density[v];
+    mass = __dmul_rn(mass, rho);
+    endep = __dmul_rn(endep, __ddiv_rn(1.602E-10, __dmul_rn(mass, nh)));
+    if (rho < 0.044) endep = 0.0;
+    t[v] = endep;
+    m = fmax(m, endep);
+  }
+  m = block_max(m, red);
+  // Non-negative doubles order like their bit patterns.
+  if (threadIdx.x == 0) atomicMax(slot_max + s, static_cast<unsigned long long>(__double_as_longlong(m)));
+}
+
+__device__ __forceinline__ double slot_threshold(const unsigned long long *slot_max, int s, double rel) {
+  return __dmul_rn(__longlong_as_double(static_cast<long long>(slot_max[s])), rel);
+}
+
+// Entries above the threshold per tile.  Grid: x over tiles, y over slots.
+__global__ void dij_count_kernel(const double *tally, long long nreg, int ntiles, const unsigned long long *slot_max,
+                                 double rel, long long *tile_count) {
+  __shared__ int red[kDijThreads / 32];
+  const int s = blockIdx.y;
+  const double thresh = slot_threshold(slot_max, s, rel);
+  const double *t = tally + static_cast<size_t>(s) * nreg + 1;
+  const long long nvox = nreg - 1;
+  const long long v0 = static_cast<long long>(blockIdx.x) * kDijTile;
+  int c = 0;
+  for (int r = 0; r < kDijRounds; r++) {
+    long long v = v0 + r * kDijThreads + threadIdx.x;
+    if (v < nvox && t[v] > thresh) c++;
+  }
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    long long sum = 0;
+    for (int w = 0; w < kDijThreads / 32; w++) sum += red[w];
+    tile_count[static_cast<size_t>(s) * ntiles + blockIdx.x] = sum;
+  }
+}
+
+// Exclusive scan of n counts by one block of 1024 threads; off[n] = total.
+__global__ void dij_scan_kernel(const long long *cnt, long long n, long long *off) {
+  __shared__ long long part[1024];
+  const int t = threadIdx.x;
+  const long long per = (n + 1023) / 1024;
+  const long long lo = t * per, hi = lo + per < n ? lo + per : n;
+  long long sum = 0;
+  for (long long i = lo; i < hi; i++) sum += cnt[i];
+  part[t] = sum;
+  __syncthreads();
+  for (int d = 1; d < 1024; d <<= 1) {
+    long long v = t >= d ? part[t - d] : 0;
+    __syncthreads();
+    part[t] += v;
+    __syncthreads();
+  }
+  long long run = part[t] - sum;
+  for (long long i = lo; i < hi; i++) {
+    off[i] = run;
+    run += cnt[i];
+  }
+  if (t == 1023) off[n] = part[1023];
+}
+
+// Rows (voxel index = region - 1) and values of the kept entries, in voxel
+// order within each slot.
+__global__ void dij_fill_kernel(const double *tally, long long nreg, int ntiles, const unsigned long long *slot_max,
+                                double rel, const long long *off, int *rows, double *vals, float *vals32) {
+  __shared__ int wtot[kDijThreads / 32];
+  const int s = blockIdx.y;
+  const double thresh = slot_threshold(slot_max, s, rel);
+  const double *t = tally + static_cast<size_t>(s) * nreg + 1;
+  const long long nvox = nreg - 1;
+  const long long v0 = static_cast<long long>(blockIdx.x) * kDijTile;
+  long long base = off[static_cast<size_t>(s) * ntiles + blockIdx.x];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int r = 0; r < kDijRounds; r++) {
+    const long long v = v0 + r * kDijThreads + threadIdx.x;
+    double d = 0.0;
+    bool keep = false;
+    if (v < nvox) {
+      d = t[v];
+      keep = d > thresh;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    if (lane == 0) wtot[warp] = __popc(m);
+    __syncthreads();
+    int wbase = 0, tot = 0;
+    for (int w = 0; w < kDijThreads / 32; w++) {
+      const int c = wtot[w];
+      if (w < warp) wbase += c;
+      tot += c;
+    }
+    if (keep) {
+      const long long o = base + wbase + __popc(m & lanemask_lt());
+      rows[o] = static_cast<int>(v);
+      if (vals) vals[o] = d;
+      else vals32[o] = static_cast<float>(d);
+    }
+    base += tot;
+    __syncthreads();
   }
 }
 
@@ -356,8 +506,21 @@ struct PrecisionState {
   Geometry<R> G{};
   Source<R> S{};
   DevBuf stk, key;
-  DevBuf queue;  // wavefront: 4 queues of 8 planes + keys
+  DevBuf queue;  // wavefront: 4 queues of 8 planes + keys (+ slot tags)
   bool tables_ok = false, geom_ok = false, source_ok = false;
+  // beamlet source (omc_engine_set_beamlets)
+  DevArrays<R> beamlets;
+  const R *bixel = nullptr, *beam_src = nullptr;
+  const int *ibeam = nullptr;
+};
+
+// Histories of one launch spread over tally slots (beamlet jobs).
+struct SlotJob {
+  int nslots;
+  const long long *first;  // device [nslots+1]
+  const int *beamlet;      // device [nslots]
+  double *tally;           // device [nslots][nreg]
+  long long nhist;         // histories of the launch
 };
 
 }  // namespace
@@ -375,6 +538,11 @@ struct omc_engine {
   int seeded_lanes = 0;  // lane count the current streams were seeded for
   // tallies and counters
   DevBuf endep, acc, acc2, counters, wf_counters;
+  // voxel densities (FP64) for the dose conversion of beamlet jobs
+  DevBuf density;
+  int nbeamlets = 0, nbeams = 0;
+  // beamlet-job buffers
+  DevBuf dij_tally, dij_first, dij_beamlet, dij_nhist, dij_max, dij_cnt, dij_off, dij_rows, dij_vals;
   // host copies needed across uploads
   omc_tables host_tables_dims{};
 };
@@ -577,9 +745,53 @@ omc_status upload_source(PrecisionState<R> &S, const omc_source *s) {
   return OMC_OK;
 }
 
+// Beamlet jobs: the launch's slot map, tally and source.
+template <typename R>
+void apply_job(Params<R> &P, const PrecisionState<R> &S, const SlotJob *job, long long nreg) {
+  P.tally_stride = nreg;
+  if (!job) return;
+  P.nslots = job->nslots;
+  P.slot_first = job->first;
+  P.slot_beamlet = job->beamlet;
+  P.endep = job->tally;
+  P.nhist = job->nhist;
+  P.S.beamlets = 1;
+  P.S.bixel = S.bixel;
+  P.S.beam_src = S.beam_src;
+  P.S.ibeam = S.ibeam;
+}
+
+template <typename R>
+omc_status upload_beamlets(PrecisionState<R> &S, const omc_beamlets *b) {
+  S.beamlets.clear();
+  std::vector<double> bix(static_cast<size_t>(b->nbeamlets) * 9), src(static_cast<size_t>(b->nbeams) * 3);
+  for (int i = 0; i < b->nbeamlets; i++) {
+    double *o = bix.data() + static_cast<size_t>(i) * 9;
+    o[0] = b->xcorner[i];
+    o[1] = b->ycorner[i];
+    o[2] = b->zcorner[i];
+    o[3] = b->xside1[i];
+    o[4] = b->yside1[i];
+    o[5] = b->zside1[i];
+    o[6] = b->xside2[i];
+    o[7] = b->yside2[i];
+    o[8] = b->zside2[i];
+  }
+  for (int i = 0; i < b->nbeams; i++) {
+    src[3 * i] = b->xsource[i];
+    src[3 * i + 1] = b->ysource[i];
+    src[3 * i + 2] = b->zsource[i];
+  }
+  S.bixel = S.beamlets.put(bix.data(), bix.size());
+  S.beam_src = S.beamlets.put(src.data(), src.size());
+  S.ibeam = S.beamlets.put_int(b->ibeam, b->nbeamlets);
+  if (!S.bixel || !S.beam_src || !S.ibeam) return fail(OMC_ERR_NOMEM, "beamlet upload failed");
+  return OMC_OK;
+}
+
 template <typename R>
 omc_status run_batches(omc_engine *e, PrecisionState<R> &S, const omc_run_config *cfg, int nlanes, int depth,
-                       omc_run_stats *stats) {
+                       omc_run_stats *stats, const SlotJob *job = nullptr) {
   size_t plane = static_cast<size_t>(depth) * nlanes;
   if (S.stk.ensure(plane * 8 * sizeof(R)) != OMC_OK) return OMC_ERR_NOMEM;
   if (S.key.ensure(plane * sizeof(int)) != OMC_OK) return OMC_ERR_NOMEM;
@@ -604,6 +816,8 @@ omc_status run_batches(omc_engine *e, PrecisionState<R> &S, const omc_run_config
   P.n_dep = &dc->n_dep;
   P.max_np = &dc->max_np;
   P.err = &dc->err;
+  apply_job(P, S, job, e->nreg);
+  const int nlaunch = job ? 1 : cfg->nbatch;
   size_t smem = kRngSmem;
   cudaFuncSetAttribute(transport_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
   int blocks = (nlanes + kBlock - 1) / kBlock;
@@ -611,9 +825,10 @@ omc_status run_batches(omc_engine *e, PrecisionState<R> &S, const omc_run_config
   cudaEventCreate(&t0);
   cudaEventCreate(&t1);
   cudaEventRecord(t0, e->stream);
-  for (int b = 0; b < cfg->nbatch; b++) {
+  for (int b = 0; b < nlaunch; b++) {
     cudaMemsetAsync(&dc->next, 0, sizeof(unsigned long long), e->stream);
     transport_kernel<R><<<blocks, kBlock, smem, e->stream>>>(P);
+    if (job) continue;
     accumulate_kernel<<<std::max(1, std::min(4 * e->nsm, (e->nreg + 255) / 256)), 256, 0, e->stream>>>(
         static_cast<double *>(e->endep.p), static_cast<double *>(e->acc.p), static_cast<double *>(e->acc2.p),
         e->nreg);
@@ -632,7 +847,7 @@ omc_status run_batches(omc_engine *e, PrecisionState<R> &S, const omc_run_config
   if (stats) {
     stats->ensrc = hc.ensrc;
     stats->transport_ms = ms;
-    stats->histories = cfg->nperbatch * cfg->nbatch;
+    stats->histories = job ? job->nhist : cfg->nperbatch * cfg->nbatch;
     stats->steps = static_cast<long long>(hc.events);
     stats->voxel_steps = static_cast<long long>(hc.n_geom);
     stats->deposits = static_cast<long long>(hc.n_dep);
@@ -665,7 +880,7 @@ int wavefront_blocks(omc_engine *e) {
 
 template <typename R>
 omc_status run_wavefront(omc_engine *e, PrecisionState<R> &S, const omc_run_config *cfg, int nlanes,
-                         omc_run_stats *stats) {
+                         omc_run_stats *stats, const SlotJob *job = nullptr) {
   const int nsplit = cfg->nsplit < 1 ? 1 : cfg->nsplit;
   const int blocks = nlanes / kBlock;
   unsigned long long target = cfg->inflight > 0 ? static_cast<unsigned long long>(cfg->inflight)
@@ -674,7 +889,8 @@ omc_status run_wavefront(omc_engine *e, PrecisionState<R> &S, const omc_run_conf
   // to two particles per split, every electron step up to two.
   unsigned long long cap = target * (4ull + 2ull * nsplit) + 4ull * nlanes;
   if (cap > 0x7fffffffull) cap = 0x7fffffffull;
-  size_t per_queue = static_cast<size_t>(cap) * (8 * sizeof(R) + sizeof(int));
+  const size_t tag_bytes = job ? static_cast<size_t>(cap) * sizeof(int) : 0;
+  size_t per_queue = static_cast<size_t>(cap) * (8 * sizeof(R) + sizeof(int)) + tag_bytes;
   if (S.queue.ensure(4 * per_queue) != OMC_OK) return OMC_ERR_NOMEM;
   if (e->wf_counters.ensure(sizeof(WfCounters)) != OMC_OK) return OMC_ERR_NOMEM;
   char *qb = static_cast<char *>(S.queue.p);
@@ -682,12 +898,15 @@ omc_status run_wavefront(omc_engine *e, PrecisionState<R> &S, const omc_run_conf
   for (int q = 0; q < 4; q++) {
     R *f = reinterpret_cast<R *>(qb + q * per_queue);
     int *k = reinterpret_cast<int *>(qb + q * per_queue + static_cast<size_t>(cap) * 8 * sizeof(R));
+    int *tag = job ? k + cap : nullptr;
     if (q < 2) {
       W.ph_f[q] = f;
       W.ph_k[q] = k;
+      W.ph_s[q] = tag;
     } else {
       W.el_f[q - 2] = f;
       W.el_k[q - 2] = k;
+      W.el_s[q - 2] = tag;
     }
   }
   WfCounters *wc = static_cast<WfCounters *>(e->wf_counters.p);
@@ -719,6 +938,8 @@ omc_status run_wavefront(omc_engine *e, PrecisionState<R> &S, const omc_run_conf
   P.n_dep = &dc->n_dep;
   P.max_np = &dc->max_np;
   P.err = &dc->err;
+  apply_job(P, S, job, e->nreg);
+  const int nlaunch = job ? 1 : cfg->nbatch;
   size_t smem = kRngSmem;
   cudaEvent_t t0, t1;
   cudaEventCreate(&t0);
@@ -726,11 +947,12 @@ omc_status run_wavefront(omc_engine *e, PrecisionState<R> &S, const omc_run_conf
   cudaEventRecord(t0, e->stream);
   int iters_total = 0;
   cudaError_t err = cudaSuccess;
-  for (int b = 0; b < cfg->nbatch && err == cudaSuccess; b++) {
+  for (int b = 0; b < nlaunch && err == cudaSuccess; b++) {
     cudaMemsetAsync(wc, 0, sizeof(WfCounters), e->stream);
     void *args[] = {&P, &W};
     err = cudaLaunchCooperativeKernel(reinterpret_cast<void *>(wavefront_kernel<R>), dim3(blocks), dim3(kBlock),
                                       args, smem, e->stream);
+    if (job) continue;
     accumulate_kernel<<<std::max(1, std::min(4 * e->nsm, (e->nreg + 255) / 256)), 256, 0, e->stream>>>(
         static_cast<double *>(e->endep.p), static_cast<double *>(e->acc.p), static_cast<double *>(e->acc2.p),
         e->nreg);
@@ -752,7 +974,7 @@ omc_status run_wavefront(omc_engine *e, PrecisionState<R> &S, const omc_run_conf
     stats->ensrc = hc.ensrc;
     stats->transport_ms = ms;
     stats->kernel_ms = ms;
-    stats->histories = cfg->nperbatch * cfg->nbatch;
+    stats->histories = job ? job->nhist : cfg->nperbatch * cfg->nbatch;
     stats->steps = static_cast<long long>(hc.events);
     stats->voxel_steps = static_cast<long long>(hc.n_geom);
     stats->deposits = static_cast<long long>(hc.n_dep);
@@ -829,6 +1051,12 @@ extern "C" void omc_engine_destroy(omc_engine *e) {
   e->acc.release();
   e->acc2.release();
   e->counters.release();
+  e->density.release();
+  e->f64.beamlets.clear();
+  e->f32.beamlets.clear();
+  for (DevBuf *b : {&e->dij_tally, &e->dij_first, &e->dij_beamlet, &e->dij_nhist, &e->dij_max, &e->dij_cnt,
+                    &e->dij_off, &e->dij_rows, &e->dij_vals})
+    b->release();
   cudaStreamDestroy(e->stream);
   delete e;
 }
@@ -875,6 +1103,9 @@ extern "C" omc_status omc_engine_set_geometry(omc_engine *e, const omc_phantom *
   if ((s = upload_geometry(e->f64, ph, med, rhof, ecut_m.data(), pcut_m.data(), nmed)) != OMC_OK) return s;
   if ((s = upload_geometry(e->f32, ph, med, rhof, ecut_m.data(), pcut_m.data(), nmed)) != OMC_OK) return s;
   e->nreg = nreg;
+  if ((s = e->density.ensure(static_cast<size_t>(nreg - 1) * sizeof(double))) != OMC_OK) return s;
+  CUDA_TRY(cudaMemcpy(e->density.p, ph->density, static_cast<size_t>(nreg - 1) * sizeof(double),
+                      cudaMemcpyHostToDevice));
   if ((s = e->endep.ensure(nreg * sizeof(double))) != OMC_OK) return s;
   if ((s = e->acc.ensure(nreg * sizeof(double))) != OMC_OK) return s;
   if ((s = e->acc2.ensure(nreg * sizeof(double))) != OMC_OK) return s;
@@ -890,22 +1121,29 @@ extern "C" omc_status omc_engine_set_source(omc_engine *e, const omc_source *s) 
   return OMC_OK;
 }
 
-static omc_status engine_run(omc_engine *e, const omc_run_config *cfg, omc_run_stats *stats) {
+// Shared start of every run: validation, schedule and lane count, RANMAR
+// streams (seeded unless continued).
+struct RunPlan {
+  bool fp64, wavefront;
+  int nlanes, depth;
+};
+
+static omc_status prepare_run(omc_engine *e, const omc_run_config *cfg, RunPlan &rp) {
   if (!e || !cfg) return fail(OMC_ERR_ARG, "null argument");
   if (!e->f64.tables_ok || !e->f64.geom_ok || !e->f64.source_ok)
     return fail(OMC_ERR_STATE, "tables, geometry and source must be set before a run");
   if (cfg->nbatch < 1 || cfg->nperbatch < 0) return fail(OMC_ERR_ARG, "nbatch must be >= 1 and nperbatch >= 0");
   if (cfg->precision != OMC_FP64 && cfg->precision != OMC_FP32) return fail(OMC_ERR_ARG, "unknown precision");
+  if (cfg->schedule < 0 || cfg->schedule > OMC_SCHEDULE_WAVEFRONT) return fail(OMC_ERR_ARG, "unknown schedule");
   omc_status s;
   if ((s = ensure_device(e)) != OMC_OK) return s;
-  const bool fp64 = cfg->precision == OMC_FP64;
-  const bool wavefront = !cfg->serial && cfg->schedule != OMC_SCHEDULE_LANES;
-  if (cfg->schedule < 0 || cfg->schedule > OMC_SCHEDULE_WAVEFRONT) return fail(OMC_ERR_ARG, "unknown schedule");
-  int nlanes;
-  if (wavefront) nlanes = (fp64 ? wavefront_blocks<double>(e) : wavefront_blocks<float>(e)) * kBlock;
-  else if (cfg->serial) nlanes = 1;
-  else nlanes = cfg->nlanes > 0 ? cfg->nlanes : (fp64 ? default_lanes<double>(e) : default_lanes<float>(e));
-  int depth = cfg->stack_depth > 0 ? cfg->stack_depth : kDefaultDepth + 4 * std::max(1, cfg->nsplit);
+  rp.fp64 = cfg->precision == OMC_FP64;
+  rp.wavefront = !cfg->serial && cfg->schedule != OMC_SCHEDULE_LANES;
+  if (rp.wavefront) rp.nlanes = (rp.fp64 ? wavefront_blocks<double>(e) : wavefront_blocks<float>(e)) * kBlock;
+  else if (cfg->serial) rp.nlanes = 1;
+  else rp.nlanes = cfg->nlanes > 0 ? cfg->nlanes : (rp.fp64 ? default_lanes<double>(e) : default_lanes<float>(e));
+  rp.depth = cfg->stack_depth > 0 ? cfg->stack_depth : kDefaultDepth + 4 * std::max(1, cfg->nsplit);
+  const int nlanes = rp.nlanes;
   // RANMAR streams, one per lane, seeded for this run.
   size_t rng_bytes = static_cast<size_t>(RNG_WORDS) * nlanes * sizeof(int);
   if (e->rng_u.n < rng_bytes) e->seeded_lanes = 0;  // reallocated: streams must be seeded
@@ -917,6 +1155,15 @@ static omc_status engine_run(omc_engine *e, const omc_run_config *cfg, omc_run_s
                                                             static_cast<int *>(e->rng_ijc.p));
     e->seeded_lanes = nlanes;
   }
+  return OMC_OK;
+}
+
+static omc_status engine_run(omc_engine *e, const omc_run_config *cfg, omc_run_stats *stats) {
+  RunPlan rp;
+  omc_status s = prepare_run(e, cfg, rp);
+  if (s != OMC_OK) return s;
+  const bool fp64 = rp.fp64, wavefront = rp.wavefront;
+  const int nlanes = rp.nlanes, depth = rp.depth;
   cudaMemsetAsync(e->endep.p, 0, e->nreg * sizeof(double), e->stream);
   cudaMemsetAsync(e->acc.p, 0, e->nreg * sizeof(double), e->stream);
   cudaMemsetAsync(e->acc2.p, 0, e->nreg * sizeof(double), e->stream);
@@ -939,6 +1186,198 @@ extern "C" omc_status omc_engine_run_resident(omc_engine *e, const omc_run_confi
   omc_status s = engine_run(e, cfg, stats);
   if (d_acc) *d_acc = static_cast<const double *>(e->acc.p);
   if (d_acc2) *d_acc2 = static_cast<const double *>(e->acc2.p);
+  return s;
+}
+
+// ---------------------------------------------------------------------------
+// Dose-influence matrix: beamlets in groups of resident tally slots.
+// ---------------------------------------------------------------------------
+extern "C" omc_status omc_engine_set_beamlets(omc_engine *e, const omc_beamlets *b) {
+  if (!e || !b) return fail(OMC_ERR_ARG, "null argument");
+  if (!e->f64.geom_ok) return fail(OMC_ERR_STATE, "omc_engine_set_geometry must come first");
+  if (b->nbeamlets < 1 || b->nbeams < 1) return fail(OMC_ERR_ARG, "need at least one beamlet and one beam");
+  if (!b->ibeam || !b->xsource || !b->ysource || !b->zsource || !b->xcorner || !b->ycorner || !b->zcorner ||
+      !b->xside1 || !b->yside1 || !b->zside1 || !b->xside2 || !b->yside2 || !b->zside2)
+    return fail(OMC_ERR_ARG, "null beamlet array");
+  for (int i = 0; i < b->nbeamlets; i++)
+    if (b->ibeam[i] < 0 || b->ibeam[i] >= b->nbeams)
+      return fail(OMC_ERR_ARG, "beamlet %d: beam %d outside 0..%d", i, b->ibeam[i], b->nbeams - 1);
+  omc_status s;
+  if ((s = ensure_device(e)) != OMC_OK) return s;
+  if ((s = upload_beamlets(e->f64, b)) != OMC_OK) return s;
+  if ((s = upload_beamlets(e->f32, b)) != OMC_OK) return s;
+  e->nbeamlets = b->nbeamlets;
+  e->nbeams = b->nbeams;
+  return OMC_OK;
+}
+
+extern "C" void omc_dij_free(omc_dij *d) {
+  if (!d) return;
+  std::free(d->col_ptr);
+  std::free(d->row_idx);
+  std::free(d->values);
+  std::free(d->values_f32);
+  std::free(d);
+}
+
+namespace {
+
+void add_stats(omc_run_stats &acc, const omc_run_stats &g) {
+  acc.ensrc += g.ensrc;
+  acc.transport_ms += g.transport_ms;
+  acc.kernel_ms += g.kernel_ms;
+  acc.histories += g.histories;
+  acc.steps += g.steps;
+  acc.voxel_steps += g.voxel_steps;
+  acc.deposits += g.deposits;
+  acc.max_stack = std::max(acc.max_stack, g.max_stack);
+  acc.error_flags |= g.error_flags;
+}
+
+omc_status run_dij(omc_engine *e, const omc_run_config *cfg, const omc_dij_config *dc, omc_dij *out,
+                   omc_run_stats *stats) {
+  RunPlan rp;
+  omc_status s = prepare_run(e, cfg, rp);
+  if (s != OMC_OK) return s;
+  const int nb = e->nbeamlets;
+  const long long nreg = e->nreg, nvox = nreg - 1;
+  std::vector<long long> nh(nb);
+  for (int b = 0; b < nb; b++) {
+    nh[b] = dc->nhist ? dc->nhist[b] : cfg->nperbatch * cfg->nbatch;
+    if (nh[b] < 1) return fail(OMC_ERR_ARG, "beamlet %d: history count %lld must be >= 1", b, nh[b]);
+  }
+  // Slots per group: the tally budget (default: 40% of free device memory,
+  // less the particle queues), at most 65535 (grid y) and nb.
+  long long budget = dc->tally_bytes;
+  if (budget <= 0) {
+    size_t fr = 0, tot = 0;
+    cudaMemGetInfo(&fr, &tot);
+    budget = static_cast<long long>(0.4 * static_cast<double>(fr));
+  }
+  long long slot_bytes = nreg * static_cast<long long>(sizeof(double));
+  long long G = budget / slot_bytes;
+  if (G < 1) G = 1;
+  if (G > nb) G = nb;
+  if (G > 65535) G = 65535;
+  const int ntiles = static_cast<int>((nvox + kDijTile - 1) / kDijTile);
+  if ((s = e->dij_tally.ensure(static_cast<size_t>(G) * slot_bytes)) != OMC_OK) return s;
+  if ((s = e->dij_first.ensure((G + 1) * sizeof(long long))) != OMC_OK) return s;
+  if ((s = e->dij_beamlet.ensure(G * sizeof(int))) != OMC_OK) return s;
+  if ((s = e->dij_nhist.ensure(G * sizeof(double))) != OMC_OK) return s;
+  if ((s = e->dij_max.ensure(G * sizeof(unsigned long long))) != OMC_OK) return s;
+  if ((s = e->dij_cnt.ensure(static_cast<size_t>(G) * ntiles * sizeof(long long))) != OMC_OK) return s;
+  if ((s = e->dij_off.ensure((static_cast<size_t>(G) * ntiles + 1) * sizeof(long long))) != OMC_OK) return s;
+
+  out->nrows = static_cast<int>(nvox);
+  out->ncols = nb;
+  out->nnz = 0;
+  out->col_ptr = static_cast<long long *>(std::calloc(static_cast<size_t>(nb) + 1, sizeof(long long)));
+  if (!out->col_ptr) return fail(OMC_ERR_NOMEM, "host allocation failed");
+  const bool f32v = dc->fp32_values != 0;
+  const size_t vsize = f32v ? sizeof(float) : sizeof(double);
+  long long host_cap = 0;
+  omc_run_stats total{};
+  omc_status worst = OMC_OK;
+  const double *xb = static_cast<const double *>(e->f64.G.xb), *yb = e->f64.G.yb, *zb = e->f64.G.zb;
+  std::vector<long long> first(G + 1), tile0(G);
+  std::vector<int> bl(G);
+  std::vector<double> nhd(G);
+  for (int g0 = 0; g0 < nb; g0 += static_cast<int>(G)) {
+    const int ng = static_cast<int>(std::min<long long>(G, nb - g0));
+    first[0] = 0;
+    for (int i = 0; i < ng; i++) {
+      first[i + 1] = first[i] + nh[g0 + i];
+      bl[i] = g0 + i;
+      nhd[i] = static_cast<double>(nh[g0 + i]);
+    }
+    cudaMemcpyAsync(e->dij_first.p, first.data(), (ng + 1) * sizeof(long long), cudaMemcpyHostToDevice, e->stream);
+    cudaMemcpyAsync(e->dij_beamlet.p, bl.data(), ng * sizeof(int), cudaMemcpyHostToDevice, e->stream);
+    cudaMemcpyAsync(e->dij_nhist.p, nhd.data(), ng * sizeof(double), cudaMemcpyHostToDevice, e->stream);
+    cudaMemsetAsync(e->dij_tally.p, 0, static_cast<size_t>(ng) * slot_bytes, e->stream);
+    cudaMemsetAsync(e->dij_max.p, 0, ng * sizeof(unsigned long long), e->stream);
+    cudaMemsetAsync(e->counters.p, 0, sizeof(Counters), e->stream);
+    SlotJob job{ng, static_cast<const long long *>(e->dij_first.p), static_cast<const int *>(e->dij_beamlet.p),
+                static_cast<double *>(e->dij_tally.p), first[ng]};
+    omc_run_stats gs{};
+    if (rp.wavefront) s = rp.fp64 ? run_wavefront(e, e->f64, cfg, rp.nlanes, &gs, &job)
+                                  : run_wavefront(e, e->f32, cfg, rp.nlanes, &gs, &job);
+    else s = rp.fp64 ? run_batches(e, e->f64, cfg, rp.nlanes, rp.depth, &gs, &job)
+                     : run_batches(e, e->f32, cfg, rp.nlanes, rp.depth, &gs, &job);
+    add_stats(total, gs);
+    if (s != OMC_OK && s != OMC_ERR_STACK && s != OMC_ERR_LIMIT) return s;
+    if (s != OMC_OK) worst = s;
+    // Dose, threshold, compaction.
+    const int bx = static_cast<int>(std::min<long long>((nvox + 255) / 256, std::max(1, 8 * e->nsm / ng + 1)));
+    double *tally = static_cast<double *>(e->dij_tally.p);
+    auto *smax = static_cast<unsigned long long *>(e->dij_max.p);
+    auto *cnt = static_cast<long long *>(e->dij_cnt.p);
+    auto *off = static_cast<long long *>(e->dij_off.p);
+    dij_dose_kernel<<<dim3(bx, ng), 256, 0, e->stream>>>(tally, nreg, e->f64.G.nx, e->f64.G.ny, xb, yb, zb,
+                                                         static_cast<const double *>(e->density.p),
+                                                         static_cast<const double *>(e->dij_nhist.p), cfg->nbatch,
+                                                         smax);
+    dij_count_kernel<<<dim3(ntiles, ng), kDijThreads, 0, e->stream>>>(tally, nreg, ntiles, smax, dc->rel_threshold,
+                                                                      cnt);
+    const long long ncnt = static_cast<long long>(ng) * ntiles;
+    dij_scan_kernel<<<1, 1024, 0, e->stream>>>(cnt, ncnt, off);
+    long long gnnz = 0;
+    CUDA_TRY(cudaMemcpyAsync(&gnnz, off + ncnt, sizeof gnnz, cudaMemcpyDeviceToHost, e->stream));
+    CUDA_TRY(cudaStreamSynchronize(e->stream));
+    if ((s = e->dij_rows.ensure((gnnz ? gnnz : 1) * sizeof(int))) != OMC_OK) return s;
+    if ((s = e->dij_vals.ensure((gnnz ? gnnz : 1) * vsize)) != OMC_OK) return s;
+    dij_fill_kernel<<<dim3(ntiles, ng), kDijThreads, 0, e->stream>>>(
+        tally, nreg, ntiles, smax, dc->rel_threshold, off, static_cast<int *>(e->dij_rows.p),
+        f32v ? nullptr : static_cast<double *>(e->dij_vals.p), f32v ? static_cast<float *>(e->dij_vals.p) : nullptr);
+    // Column starts: the offset of each slot's first tile.
+    CUDA_TRY(cudaMemcpy2DAsync(tile0.data(), sizeof(long long), off, static_cast<size_t>(ntiles) * sizeof(long long),
+                               sizeof(long long), ng, cudaMemcpyDeviceToHost, e->stream));
+    if (out->nnz + gnnz > host_cap) {
+      long long cap = std::max(out->nnz + gnnz, 2 * host_cap);
+      int *r = static_cast<int *>(std::realloc(out->row_idx, (cap ? cap : 1) * sizeof(int)));
+      if (r) out->row_idx = r;
+      void *v = std::realloc(f32v ? static_cast<void *>(out->values_f32) : static_cast<void *>(out->values),
+                             (cap ? cap : 1) * vsize);
+      if (v) {
+        if (f32v) out->values_f32 = static_cast<float *>(v);
+        else out->values = static_cast<double *>(v);
+      }
+      if (!r || !v) return fail(OMC_ERR_NOMEM, "host allocation of %lld dij entries failed", cap);
+      host_cap = cap;
+    }
+    if (gnnz > 0) {
+      CUDA_TRY(cudaMemcpyAsync(out->row_idx + out->nnz, e->dij_rows.p, gnnz * sizeof(int), cudaMemcpyDeviceToHost,
+                               e->stream));
+      void *vdst = f32v ? static_cast<void *>(out->values_f32 + out->nnz) : static_cast<void *>(out->values + out->nnz);
+      CUDA_TRY(cudaMemcpyAsync(vdst, e->dij_vals.p, gnnz * vsize, cudaMemcpyDeviceToHost, e->stream));
+    }
+    CUDA_TRY(cudaStreamSynchronize(e->stream));
+    CUDA_TRY(cudaGetLastError());
+    for (int i = 0; i < ng; i++) out->col_ptr[g0 + i] = out->nnz + tile0[i];
+    out->nnz += gnnz;
+    out->col_ptr[g0 + ng] = out->nnz;
+  }
+  if (stats) *stats = total;
+  if (worst == OMC_ERR_STACK) return fail(OMC_ERR_STACK, "particle stack or queue overflow; histories were dropped");
+  if (worst == OMC_ERR_LIMIT) return fail(OMC_ERR_LIMIT, "a device loop hit its iteration limit");
+  return OMC_OK;
+}
+
+}  // namespace
+
+extern "C" omc_status omc_engine_run_dij(omc_engine *e, const omc_run_config *cfg, const omc_dij_config *dcfg,
+                                         omc_dij **out, omc_run_stats *stats) {
+  if (!e || !cfg || !dcfg || !out) return fail(OMC_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (e->nbeamlets < 1) return fail(OMC_ERR_STATE, "omc_engine_set_beamlets must come first");
+  if (!(dcfg->rel_threshold >= 0.0)) return fail(OMC_ERR_ARG, "relative dose threshold must be >= 0");
+  auto *d = static_cast<omc_dij *>(std::calloc(1, sizeof(omc_dij)));
+  if (!d) return fail(OMC_ERR_NOMEM, "host allocation failed");
+  omc_status s = run_dij(e, cfg, dcfg, d, stats);
+  if (s != OMC_OK && s != OMC_ERR_STACK && s != OMC_ERR_LIMIT) {
+    omc_dij_free(d);
+    return s;
+  }
+  *out = d;
   return s;
 }
 

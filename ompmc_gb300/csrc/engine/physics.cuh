@@ -38,6 +38,13 @@ __device__ __forceinline__ V4<double> ld4(const V4<double> *p) {
   return V4<double>{a.x, a.y, b.x, b.y};
 }
 
+// Separately rounded products and sums (never fused into an FMA), where a
+// one-ulp difference from the reference's arithmetic matters.
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+
 // Output queues of the current wavefront phase.
 template <typename R>
 struct EmitTargets {
@@ -47,6 +54,7 @@ struct EmitTargets {
   R *el_f;
   int *el_k;
   unsigned *el_n;
+  int *ph_s, *el_s;   // tally slots [cap] (beamlet jobs only)
 };
 
 __device__ __forceinline__ unsigned lanemask_lt() {
@@ -60,7 +68,8 @@ struct Lane {
   const Params<R> &P;
   Ranmar rng;
   int lane;
-  int np;  // top slot, -1 = empty (per-lane schedule)
+  int slot;  // tally slot of the current history / particle (beamlet jobs)
+  int np;    // top slot, -1 = empty (per-lane schedule)
   Particle<R> p;
   bool alive;           // wavefront: p still needs to be queued
   EmitTargets<R> out;   // wavefront: where this phase appends
@@ -78,6 +87,7 @@ struct Lane {
     rng.hi = shi;
     rng.stride = sstride;
     np = -1;
+    slot = 0;
     ensrc = 0.0;
     err = 0;
     max_np = 0;
@@ -154,7 +164,7 @@ struct Lane {
 
   // Wavefront append: lanes that emit together share one atomic per queue
   // (ballot + popc), so a warp writes consecutive, coalesced slots.
-  __device__ __forceinline__ void emit_to(R *f, int *k, unsigned *n, const Particle<R> &q) {
+  __device__ __forceinline__ void emit_to(R *f, int *k, unsigned *n, const Particle<R> &q, int *tag) {
     unsigned m = __activemask();
     int leader = __ffs(m) - 1;
     unsigned base = 0;
@@ -176,12 +186,14 @@ struct Lane {
     __stcg(f + 6 * c + slot, q.w);
     __stcg(f + 7 * c + slot, q.wt);
     __stcg(k + slot, q.ir * 4 + (q.iq + 1));
+    if (tag) __stcg(tag + slot, this->slot);
   }
   __device__ __forceinline__ void emit(const Particle<R> &q) {
-    if (q.iq == 0) emit_to(out.ph_f, out.ph_k, out.ph_n, q);
-    else emit_to(out.el_f, out.el_k, out.el_n, q);
+    if (q.iq == 0) emit_to(out.ph_f, out.ph_k, out.ph_n, q, out.ph_s);
+    else emit_to(out.el_f, out.el_k, out.el_n, q, out.el_s);
   }
-  __device__ __forceinline__ void take(const R *f, const int *k, unsigned slot) {
+  __device__ __forceinline__ void take(const R *f, const int *k, unsigned slot, const int *tag) {
+    if (tag) this->slot = __ldcg(tag + slot);
     size_t c = queue_cap;
     p.e = __ldcg(f + slot);
     p.x = __ldcg(f + c + slot);
@@ -200,7 +212,7 @@ struct Lane {
   // ---- scoring: ausgab (omc_dosxyz.c:683-694) ------------------------------
   __device__ __forceinline__ void ausgab(int ir, R wt, R edep) {
     n_dep++;
-    atomicAdd(P.endep + ir, static_cast<double>(wt * edep));
+    atomicAdd(P.endep + static_cast<size_t>(slot) * P.tally_stride + ir, static_cast<double>(wt * edep));
   }
 
   // ---- geometry: region decode, howfar, hownear (omc_dosxyz.c:187-334) ----
@@ -372,11 +384,11 @@ struct Lane {
 #include "photon.inc"
 #include "electron.inc"
 
-  // ---- source: initHistory (omc_dosxyz.c:964-1068) --------------------------
-  __device__ void init_history() {
+  // ---- source -------------------------------------------------------------
+  // Energy and charge of a new history (initHistory's first part, the same
+  // in omc_dosxyz.c:970-996 and omc_matrad.c:1092-1123).
+  __device__ __forceinline__ void source_energy(Particle<R> &q) {
     const Source<R> &s = P.S;
-    const Geometry<R> &g = P.G;
-    Particle<R> q;
     q.iq = s.charge;
     R ein;
     if (s.spectrum) {
@@ -389,6 +401,104 @@ struct Lane {
     }
     q.e = (q.iq != 0) ? ein + RC(0.5109989461) : ein;
     ensrc += static_cast<double>(ein);
+  }
+
+  // History h of the launch: its tally slot (beamlet jobs), then the
+  // source particle.
+  __device__ void init_history(long long h) {
+    if (P.nslots > 0) {
+      int lo = 0, hi = P.nslots - 1;
+      while (lo < hi) {  // last slot whose first history is <= h
+        int mid = (lo + hi + 1) >> 1;
+        if (__ldg(P.slot_first + mid) <= h) lo = mid;
+        else hi = mid - 1;
+      }
+      slot = lo;
+    }
+    if (P.S.beamlets) init_beamlet_history(__ldg(P.slot_beamlet + slot));
+    else init_point_history();
+  }
+
+  // initHistory(ibeamlet) (omc_matrad.c:1084-1254): a uniform point of the
+  // bixel, moved back along the line to the beam's source point onto the
+  // phantom surface, heading into the phantom.  The reference clamps z
+  // against ybounds[0] (:1225); that is kept.  A point that lands a
+  // rounding error below zbounds[0] is moved by that clamp, so the
+  // arithmetic here is rounded operation by operation like the
+  // reference's (no fused multiply-adds).
+  __device__ void init_beamlet_history(int ib) {
+    const Source<R> &s = P.S;
+    const Geometry<R> &g = P.G;
+    Particle<R> q;
+    source_energy(q);
+    R rnno1 = rnd();
+    R rnno2 = rnd();
+    const R *b = s.bixel + static_cast<size_t>(ib) * 9;
+    R xiso = add_rn(add_rn(mul_rn(rnno1, __ldg(b + 3)), mul_rn(rnno2, __ldg(b + 6))), __ldg(b + 0));
+    R yiso = add_rn(add_rn(mul_rn(rnno1, __ldg(b + 4)), mul_rn(rnno2, __ldg(b + 7))), __ldg(b + 1));
+    R ziso = add_rn(add_rn(mul_rn(rnno1, __ldg(b + 5)), mul_rn(rnno2, __ldg(b + 8))), __ldg(b + 2));
+    const R *src = s.beam_src + 3 * __ldg(s.ibeam + ib);
+    R dx = xiso - __ldg(src + 0), dy = yiso - __ldg(src + 1), dz = ziso - __ldg(src + 2);
+    R vnorm = sqrt(add_rn(add_rn(mul_rn(dx, dx), mul_rn(dy, dy)), mul_rn(dz, dz)));
+    R u = -dx / vnorm, v = -dy / vnorm, w = -dz / vnorm;
+    R ustep = RC(1.0E5), dist;
+    const R x0 = __ldg(g.xb), x1 = __ldg(g.xb + g.nx);
+    const R y0 = __ldg(g.yb), y1 = __ldg(g.yb + g.ny);
+    const R z0 = __ldg(g.zb), z1 = __ldg(g.zb + g.nz);
+    if (u > RC(0)) {
+      dist = (x1 - xiso) / u;
+      if (dist < ustep) ustep = dist;
+    }
+    if (u < RC(0)) {
+      dist = -(xiso - x0) / u;
+      if (dist < ustep) ustep = dist;
+    }
+    if (v > RC(0)) {
+      dist = (y1 - yiso) / v;
+      if (dist < ustep) ustep = dist;
+    }
+    if (v < RC(0)) {
+      dist = -(yiso - y0) / v;
+      if (dist < ustep) ustep = dist;
+    }
+    if (w > RC(0)) {
+      dist = (z1 - ziso) / w;
+      if (dist < ustep) ustep = dist;
+    }
+    if (w < RC(0)) {
+      dist = -(ziso - z0) / w;
+      if (dist < ustep) ustep = dist;
+    }
+    R x = add_rn(xiso, mul_rn(ustep, u)), y = add_rn(yiso, mul_rn(ustep, v)), z = add_rn(ziso, mul_rn(ustep, w));
+    q.u = -u;
+    q.v = -v;
+    q.w = -w;
+    const R tiny = RC(2.0 * 2.2250738585072014e-308);  // 2*DBL_MIN
+    if (x < x0) x = x0 + tiny;
+    if (x > x1) x = x1 - tiny;
+    if (y < y0) y = y0 + tiny;
+    if (y > y1) y = y1 - tiny;
+    if (z < z0) z = y0 + tiny;
+    if (z > z1) z = z1 - tiny;
+    q.x = x;
+    q.y = y;
+    q.z = z;
+    int ix = 0, iy = 0, iz = 0;
+    while (ix < g.nx - 1 && __ldg(g.xb + ix + 1) < x) ix++;
+    while (iy < g.ny - 1 && __ldg(g.yb + iy + 1) < y) iy++;
+    while (iz < g.nz - 1 && __ldg(g.zb + iz + 1) < z) iz++;
+    q.ir = 1 + ix + iy * g.nx + iz * g.nxy;
+    q.wt = RC(1);
+    p = q;
+    np = 0;
+  }
+
+  // initHistory (omc_dosxyz.c:964-1068): collimated point source.
+  __device__ void init_point_history() {
+    const Source<R> &s = P.S;
+    const Geometry<R> &g = P.G;
+    Particle<R> q;
+    source_energy(q);
     R rxyz;
     if (s.xsize == RC(0) || s.ysize == RC(0)) {
       q.x = s.xinl;

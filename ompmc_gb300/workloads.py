@@ -106,6 +106,59 @@ def ct_like(nx=256, ny=256, nz=128, vox=0.2, nblobs=40, seed=2024):
     return Phantom(media, xb, yb, zb, med, rho)
 
 
+@dataclass
+class Beamlets:
+    """matRad-style pencil beamlets (the mcSrc fields of omc_matrad):
+    bixel k is corner[k] + a*side1[k] + b*side2[k], a, b in [0, 1), at the
+    isocentre plane, irradiated from source[ibeam[k]]."""
+
+    ibeam: np.ndarray   # int32 [n], 0-based beam index
+    source: np.ndarray  # [nbeams, 3]
+    corner: np.ndarray  # [n, 3]
+    side1: np.ndarray   # [n, 3]
+    side2: np.ndarray   # [n, 3]
+
+    @property
+    def n(self):
+        return int(len(self.ibeam))
+
+
+def beamlets(gantry_deg=(0.0,), iso=(0.0, 0.0, 15.0), sad=100.0, bixel=0.5, field=10.0, radius=None):
+    """Bixel grids for beams at the given gantry angles.  Gantry angle g
+    rotates the beam about the y axis through the isocentre: the source is
+    at iso - sad*(sin g, 0, cos g), so g = 0 irradiates along +z.  Each
+    beam carries a field x field cm grid of bixel x bixel cm bixels at the
+    isocentre plane, restricted to bixels whose centre lies within
+    `radius` of the axis when given."""
+    iso = np.asarray(iso, dtype=np.float64)
+    n1 = int(round(field / bixel))
+    ib, src, cor, s1, s2 = [], [], [], [], []
+    for b, g in enumerate(gantry_deg):
+        t = np.deg2rad(g)
+        axis = np.array([np.sin(t), 0.0, np.cos(t)])
+        e1 = np.array([np.cos(t), 0.0, -np.sin(t)])
+        e2 = np.array([0.0, 1.0, 0.0])
+        src.append(iso - sad * axis)
+        for i in range(n1):
+            for j in range(n1):
+                a = -0.5 * field + i * bixel
+                c = -0.5 * field + j * bixel
+                if radius is not None and np.hypot(a + 0.5 * bixel, c + 0.5 * bixel) > radius:
+                    continue
+                ib.append(b)
+                cor.append(iso + a * e1 + c * e2)
+                s1.append(bixel * e1)
+                s2.append(bixel * e2)
+    return Beamlets(np.array(ib, np.int32), np.array(src), np.array(cor), np.array(s1), np.array(s2))
+
+
+def lognormal_histories(n, median=5e4, sigma=1.0, lo=1e4, hi=1e6, seed=7):
+    """Histories per beamlet: lognormal with the given median and log
+    standard deviation, clipped to [lo, hi], from default_rng(seed)."""
+    rng = np.random.default_rng(seed)
+    return np.clip(np.round(median * np.exp(sigma * rng.standard_normal(n))), lo, hi).astype(np.int64)
+
+
 def write_egsphant(ph: Phantom, path: str) -> str:
     nz, ny, nx = ph.shape
     lines = [str(len(ph.media))] + list(ph.media) + ["  ".join(["0.25"] * len(ph.media)),

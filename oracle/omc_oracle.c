@@ -7,6 +7,7 @@
  */
 #include "omc_oracle.h"
 
+#include <float.h>
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -100,6 +101,7 @@ typedef struct {
     const omc_source *src;
     int nsplit;
     double *endep; /* batch tally, shared between threads */
+    const omc_beamlets *bl; /* beamlet source (omc_matrad), or NULL */
 } ctx_t;
 
 typedef struct {
@@ -1799,7 +1801,7 @@ int omc_oracle_run(const omc_tables *t, const omc_phantom *ph, const omc_regions
     if (!endep) return 2;
     memset(accum_endep, 0, nreg * sizeof(double));
     memset(accum_endep2, 0, nreg * sizeof(double));
-    ctx_t c = {t, ph, rg, src, nsplit < 1 ? 1 : nsplit, endep};
+    ctx_t c = {t, ph, rg, src, nsplit < 1 ? 1 : nsplit, endep, NULL};
 #ifdef _OPENMP
     if (nthreads <= 0) nthreads = omp_get_num_procs();
 #else
@@ -1860,4 +1862,227 @@ int omc_oracle_run(const omc_tables *t, const omc_phantom *ph, const omc_regions
         res->status = overflow;
     }
     return overflow;
+}
+
+/* ---------------------------------------------------------------------- */
+/* omc_matrad: beamlet source and dose-influence matrix.                    */
+
+/* initHistory(ibeamlet) (ucodes/omc_matrad/omc_matrad.c:1084-1254): energy
+ * as in omc_dosxyz, a uniform point on the beamlet's bixel, moved back
+ * along the line to its beam's source point onto the phantom surface, and
+ * the voxel found by linear scans.  The reference clamps z against
+ * ybounds[0] (:1225); that is kept. */
+static void init_beamlet_history(track_t *tk, int ib) {
+    const omc_source *s = tk->c->src;
+    const omc_beamlets *b = tk->c->bl;
+    const omc_phantom *g = tk->c->ph;
+    tk->np = 0;
+    tk->iq[0] = s->charge;
+    double ein;
+    if (s->spectrum) {
+        double rnno1 = rnd(tk);
+        double rnno2 = rnd(tk);
+        int k = (int)fmin(s->deltak * rnno1, s->deltak - 1.0);
+        ein = s->cdfinv1[k] + rnno2 * s->cdfinv2[k];
+    } else {
+        ein = s->energy;
+    }
+    tk->e[0] = (tk->iq[0] != 0) ? ein + RM : ein;
+    tk->ensrc += ein;
+    double rnno1 = rnd(tk);
+    double rnno2 = rnd(tk);
+    double xiso = rnno1 * b->xside1[ib] + rnno2 * b->xside2[ib] + b->xcorner[ib];
+    double yiso = rnno1 * b->yside1[ib] + rnno2 * b->yside2[ib] + b->ycorner[ib];
+    double ziso = rnno1 * b->zside1[ib] + rnno2 * b->zside2[ib] + b->zcorner[ib];
+    int ibeam = b->ibeam[ib];
+    double vnorm = sqrt(pow(xiso - b->xsource[ibeam], 2.0) + pow(yiso - b->ysource[ibeam], 2.0) +
+                        pow(ziso - b->zsource[ibeam], 2.0));
+    double u = -(xiso - b->xsource[ibeam]) / vnorm;
+    double v = -(yiso - b->ysource[ibeam]) / vnorm;
+    double w = -(ziso - b->zsource[ibeam]) / vnorm;
+    double ustep = 1.0E5, dist;
+    if (u > 0.0) {
+        dist = (g->xbounds[g->nx] - xiso) / u;
+        if (dist < ustep) ustep = dist;
+    }
+    if (u < 0.0) {
+        dist = -(xiso - g->xbounds[0]) / u;
+        if (dist < ustep) ustep = dist;
+    }
+    if (v > 0.0) {
+        dist = (g->ybounds[g->ny] - yiso) / v;
+        if (dist < ustep) ustep = dist;
+    }
+    if (v < 0.0) {
+        dist = -(yiso - g->ybounds[0]) / v;
+        if (dist < ustep) ustep = dist;
+    }
+    if (w > 0.0) {
+        dist = (g->zbounds[g->nz] - ziso) / w;
+        if (dist < ustep) ustep = dist;
+    }
+    if (w < 0.0) {
+        dist = -(ziso - g->zbounds[0]) / w;
+        if (dist < ustep) ustep = dist;
+    }
+    double x = xiso + ustep * u, y = yiso + ustep * v, z = ziso + ustep * w;
+    tk->u[0] = -u;
+    tk->v[0] = -v;
+    tk->w[0] = -w;
+    if (x < g->xbounds[0]) x = g->xbounds[0] + 2.0 * DBL_MIN;
+    if (x > g->xbounds[g->nx]) x = g->xbounds[g->nx] - 2.0 * DBL_MIN;
+    if (y < g->ybounds[0]) y = g->ybounds[0] + 2.0 * DBL_MIN;
+    if (y > g->ybounds[g->ny]) y = g->ybounds[g->ny] - 2.0 * DBL_MIN;
+    if (z < g->zbounds[0]) z = g->ybounds[0] + 2.0 * DBL_MIN;
+    if (z > g->zbounds[g->nz]) z = g->zbounds[g->nz] - 2.0 * DBL_MIN;
+    tk->x[0] = x;
+    tk->y[0] = y;
+    tk->z[0] = z;
+    int ix = 0, iy = 0, iz = 0;
+    while (g->xbounds[ix + 1] < x) ix++;
+    while (g->ybounds[iy + 1] < y) iy++;
+    while (g->zbounds[iz + 1] < z) iz++;
+    tk->ir[0] = 1 + ix + iy * g->nx + iz * g->nx * g->ny;
+    tk->wt[0] = 1.0;
+    tk->dnear[0] = 0.0;
+}
+
+/* Dose of one beamlet from its batch sums, then threshold and column of
+ * the CSC matrix (omc_matrad.c:839-919 accumulateResults with iout = 1,
+ * :1426-1482 threshold and column fill). */
+static int dij_column(const omc_phantom *ph, const double *accum, long long nhist, int nbatch, double rel,
+                      double *dose, omc_dij *d, long long *cap, int col) {
+    int nx = ph->nx, ny = ph->ny, nz = ph->nz;
+    long long nvox = (long long)nx * ny * nz;
+    double inc_fluence = (double)nhist;
+    for (int iz = 0; iz < nz; iz++)
+        for (int iy = 0; iy < ny; iy++)
+            for (int ix = 0; ix < nx; ix++) {
+                long long irl = 1 + ix + (long long)iy * nx + (long long)iz * nx * ny;
+                double endep = accum[irl] / (double)nbatch;
+                if (endep == 0.0) endep = 0.0;
+                double mass = (ph->xbounds[ix + 1] - ph->xbounds[ix]) * (ph->ybounds[iy + 1] - ph->ybounds[iy]) *
+                              (ph->zbounds[iz + 1] - ph->zbounds[iz]);
+                mass *= ph->density[irl - 1];
+                endep *= 1.602E-10 / (mass * inc_fluence);
+                if (ph->density[irl - 1] < 0.044) endep = 0.0;
+                dose[irl] = endep;
+            }
+    double dmax = 0.0;
+    for (long long irl = 1; irl < nvox + 1; irl++)
+        if (dose[irl] > dmax) dmax = dose[irl];
+    double thresh = dmax * rel;
+    long long nnz = 0;
+    for (long long irl = 1; irl < nvox + 1; irl++)
+        if (dose[irl] > thresh) nnz++;
+    if (d->nnz + nnz > *cap) {
+        long long nc = (d->nnz + nnz) * 2 + 16;
+        int *ri = realloc(d->row_idx, nc * sizeof(int));
+        double *va = realloc(d->values, nc * sizeof(double));
+        if (!ri || !va) return 2;
+        d->row_idx = ri;
+        d->values = va;
+        *cap = nc;
+    }
+    for (long long irl = 1; irl < nvox + 1; irl++)
+        if (dose[irl] > thresh) {
+            d->row_idx[d->nnz] = (int)(irl - 1);
+            d->values[d->nnz] = dose[irl];
+            d->nnz++;
+        }
+    d->col_ptr[col + 1] = d->nnz;
+    return 0;
+}
+
+int omc_oracle_run_dij(const omc_tables *t, const omc_phantom *ph, const omc_regions *rg, const omc_source *src,
+                       const omc_beamlets *bl, int nsplit, const long long *nhist, long long nperbatch, int nbatch,
+                       int ixx, int jxx, int nthreads, double rel_threshold, omc_dij *out, omc_oracle_result *res) {
+    int nreg = rg->nreg;
+    memset(out, 0, sizeof *out);
+    out->nrows = nreg - 1;
+    out->ncols = bl->nbeamlets;
+    out->col_ptr = calloc((size_t)bl->nbeamlets + 1, sizeof(long long));
+    double *endep = calloc(nreg, sizeof(double));
+    double *accum = calloc(nreg, sizeof(double));
+    double *dose = calloc(nreg, sizeof(double));
+    if (!endep || !accum || !dose || !out->col_ptr) return 2;
+    ctx_t c = {t, ph, rg, src, nsplit < 1 ? 1 : nsplit, endep, bl};
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_num_procs();
+#else
+    nthreads = 1;
+#endif
+    track_t **tks = calloc(nthreads, sizeof(track_t *));
+    for (int i = 0; i < nthreads; i++) {
+        tks[i] = calloc(1, sizeof(track_t));
+        tks[i]->c = &c;
+        ranmar_init(&tks[i]->rng, ixx, jxx + (nthreads > 1 ? i : 0));
+    }
+#ifdef _OPENMP
+    double t0 = omp_get_wtime();
+#endif
+    long long cap = 0, total = 0;
+    int status = 0;
+    for (int ib = 0; ib < bl->nbeamlets && !status; ib++) {
+        /* Histories of this beamlet: nbatch batches of nhist/nbatch
+         * (omc_matrad.c:1321-1335 and the loop at :1389-1404). */
+        long long nb = nhist ? nhist[ib] : nperbatch * nbatch;
+        long long per = nb / nbatch;
+        if (per == 0) per = 1;
+        for (int batch = 0; batch < nbatch; batch++) {
+            if (nthreads > 1) {
+                #pragma omp parallel for schedule(dynamic) num_threads(nthreads)
+                for (long long ih = 0; ih < per; ih++) {
+#ifdef _OPENMP
+                    track_t *tk = tks[omp_get_thread_num()];
+#else
+                    track_t *tk = tks[0];
+#endif
+                    init_beamlet_history(tk, ib);
+                    shower(tk);
+                }
+            } else {
+                for (long long ih = 0; ih < per; ih++) {
+                    init_beamlet_history(tks[0], ib);
+                    shower(tks[0]);
+                }
+            }
+            for (int r = 0; r < nreg; r++) accum[r] += endep[r];
+            memset(endep, 0, nreg * sizeof(double));
+        }
+        total += per * nbatch;
+        status = dij_column(ph, accum, per * nbatch, nbatch, rel_threshold, dose, out, &cap, ib);
+        memset(accum, 0, nreg * sizeof(double));
+    }
+    double ens = 0.0;
+    int overflow = 0;
+    for (int i = 0; i < nthreads; i++) {
+        ens += tks[i]->ensrc;
+        overflow |= tks[i]->overflow;
+        free(tks[i]);
+    }
+    free(tks);
+    free(endep);
+    free(accum);
+    free(dose);
+    if (res) {
+        res->ensrc = ens;
+#ifdef _OPENMP
+        res->seconds = omp_get_wtime() - t0;
+#else
+        res->seconds = 0.0;
+#endif
+        res->histories = total;
+        res->nthreads = nthreads;
+        res->status = overflow;
+    }
+    return status ? status : overflow;
+}
+
+void omc_oracle_dij_free(omc_dij *d) {
+    if (!d) return;
+    free(d->col_ptr);
+    free(d->row_idx);
+    free(d->values);
+    memset(d, 0, sizeof *d);
 }

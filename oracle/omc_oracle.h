@@ -46,6 +46,21 @@ int omc_oracle_run(const omc_tables *t, const omc_phantom *ph,
                    int nthreads, double *accum_endep, double *accum_endep2,
                    omc_oracle_result *res);
 
+/* The omc_matrad beamlet loop (ucodes/omc_matrad/omc_matrad.c:1374-1512):
+ * beamlet by beamlet, nbatch batches of (nhist[ib] or nperbatch*nbatch)/
+ * nbatch histories from the beamlet source (initHistory(ibeamlet),
+ * :1084-1254), then the beamlet's dose (accumulateResults, :839-919),
+ * threshold and CSC column.  out's arrays are malloc'd; release them with
+ * omc_oracle_dij_free.  Returns 0 on success. */
+int omc_oracle_run_dij(const omc_tables *t, const omc_phantom *ph,
+                       const omc_regions *rg, const omc_source *src,
+                       const omc_beamlets *bl, int nsplit,
+                       const long long *nhist, long long nperbatch,
+                       int nbatch, int ixx, int jxx, int nthreads,
+                       double rel_threshold, omc_dij *out,
+                       omc_oracle_result *res);
+void omc_oracle_dij_free(omc_dij *d);
+
 /* n numbers of the RANMAR stream seeded (ixx, jxx) as 24-bit integers. */
 void omc_oracle_ranmar(int ixx, int jxx, long long n, int *out);
 

@@ -38,7 +38,8 @@ CASES = {
 }
 
 
-def write_case(name: str, directory: str, ncase: int | None = None, nbatch: int = 10, seeds=(97, 33)) -> str:
+def write_case(name: str, directory: str, ncase: int | None = None, nbatch: int = 10, seeds=(97, 33),
+               nsplit: int | None = None) -> str:
     """Write the case's .egsphant/.spectrum/.inp into directory; returns the
     input path without the .inp extension."""
     builder, kw = CASES[name]
@@ -58,6 +59,8 @@ def write_case(name: str, directory: str, ncase: int | None = None, nbatch: int 
                                          *W.spectrum_250kvp())
     if ncase is not None:
         kw["ncase"] = ncase
+    if nsplit is not None:
+        kw["nsplit"] = nsplit
     job = W.Job(phant, P["pegs"], P["pgs4form"], P["data_folder"], directory + os.sep,
                 spectrum_file=spectrum_file, nbatch=nbatch, seeds=seeds, **kw)
     return job.write(os.path.join(directory, name))
@@ -65,3 +68,36 @@ def write_case(name: str, directory: str, ncase: int | None = None, nbatch: int 
 
 RANMAR_SEEDS = [(97, 33), (97, 34), (1802, 9373), (12, 31328), (31328, 1), (5, 17)]
 RANMAR_N = 2000
+
+
+# Beamlet (omc_matrad) cases: name -> (dose case, job keywords, beamlet
+# keywords, relative dose threshold).  The reference's matRad front end
+# always reads a spectrum file, so both use the synthetic 6 MV spectrum.
+DIJ_CASES = {
+    "dij_slab": ("slab_6mv", dict(ncase=300, nbatch=3, nsplit=1),
+                 dict(gantry_deg=(0.0, 90.0, 51.43), bixel=1.0, field=3.0, radius=1.6), 1e-4),
+    "dij_split": ("slab_6mv", dict(ncase=200, nbatch=2, nsplit=3),
+                  dict(gantry_deg=(180.0, 308.57), bixel=1.0, field=3.0, radius=1.6), 1e-2),
+}
+
+
+def dij_case(name: str, directory: str, ncase: int | None = None, nbatch: int | None = None, seeds=(97, 33)):
+    """Write the dose case behind a beamlet case; returns (input path
+    without .inp, phantom, beamlets, mcOpt fields for the reference's
+    matRad front end, relative threshold, nsplit)."""
+    from ompmc_gb300 import workloads as W2
+
+    base, job, bkw, thr = DIJ_CASES[name]
+    ncase = job["ncase"] if ncase is None else ncase
+    nbatch = job["nbatch"] if nbatch is None else nbatch
+    inp = write_case(base, directory, ncase=ncase, nbatch=nbatch, seeds=seeds, nsplit=job["nsplit"])
+    ph = CASES[base][0]()
+    zc = 0.5 * (ph.zb[0] + ph.zb[-1])
+    bl = W2.beamlets(iso=(0.3, -0.2, zc), sad=100.0, **bkw)
+    P = data.paths()
+    opts = dict(nHistories=ncase, nBatches=nbatch, nSplit=job["nsplit"],
+                spectrumFile=os.path.join(directory, base + ".spectrum"), monoEnergy=1.25, charge=0,
+                global_ecut=0.7, global_pcut=0.01, randomSeeds=list(seeds), pegsFile=P["pegs"],
+                pgs4formFile=P["pgs4form"], dataFolder=P["data_folder"], outputFolder=directory + os.sep,
+                relDoseThreshold=thr, verbose=0)
+    return inp, ph, bl, opts, thr, job["nsplit"]

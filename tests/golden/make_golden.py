@@ -10,6 +10,10 @@ needs the reference source tree) through oracle/ref_harness.c and stores:
   dose_<case>.npz   raw batch sums accum_endep / accum_endep2 and the source
                     energy of the reference's serial build for each case in
                     tests.cases.CASES
+  <dij case>.npz    the sparse dose-influence matrix (jc, ir, pr) the
+                    reference's omc_matrad front end returns (serial build,
+                    run outside MATLAB by oracle/matrad_harness.c) for each
+                    case in tests.cases.DIJ_CASES
 
 Usage:  python tests/golden/make_golden.py
 """
@@ -29,7 +33,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.dirname(HERE))
 
-from cases import CASES, RANMAR_N, RANMAR_SEEDS, write_case  # noqa: E402
+from cases import CASES, DIJ_CASES, RANMAR_N, RANMAR_SEEDS, dij_case, write_case  # noqa: E402
 
 from ompmc_gb300 import data  # noqa: E402
 from oracle import binding as O  # noqa: E402
@@ -48,7 +52,7 @@ def table_digests(d):
 
 
 def main():
-    if not O.ref_available():
+    if not (O.ref_available() and O.ref_matrad_available()):
         raise SystemExit("reference not built: run `make -C oracle ref` where the reference tree is present")
     data.stage()
     with tempfile.TemporaryDirectory() as tmp:
@@ -65,6 +69,12 @@ def main():
                                 accum_endep2=d["accum_endep2"], ensrc=d["ensrc"], nperbatch=d["nperbatch"],
                                 nbatch=d["nbatch"])
             print(name, "ensrc", d["ensrc"][0], "edep", d["accum_endep"][1:].sum())
+        for name in DIJ_CASES:
+            d = os.path.join(tmp, name)
+            _, ph, bl, opts, _, _ = dij_case(name, d)
+            jc, ir, pr = O.ref_matrad(os.path.join(d, "ref"), ph, bl, opts)
+            np.savez_compressed(os.path.join(HERE, f"{name}.npz"), jc=jc, ir=ir, pr=pr)
+            print(name, "beamlets", bl.n, "nnz", len(pr))
 
 
 if __name__ == "__main__":

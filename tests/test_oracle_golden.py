@@ -7,7 +7,7 @@ import os
 
 import numpy as np
 import pytest
-from cases import CASES, RANMAR_N, RANMAR_SEEDS, write_case
+from cases import CASES, DIJ_CASES, RANMAR_N, RANMAR_SEEDS, dij_case, write_case
 from conftest import GOLDEN
 
 
@@ -113,3 +113,42 @@ def test_oracle_threads_statistically_consistent(oracle, problem_factory):
     tot1, tot4 = a1[1:].sum(), a4[1:].sum()
     # batch estimate of the total's standard deviation
     assert abs(tot1 - tot4) < 0.03 * tot1
+
+
+@pytest.mark.parametrize("name", sorted(DIJ_CASES))
+def test_serial_dij_bit_exact_with_reference(name, oracle, native, tmp_path):
+    """The oracle's beamlet loop == the reference's omc_matrad front end
+    (serial build, run outside MATLAB): same columns, rows and values."""
+    import platform
+
+    from ompmc_gb300 import api
+
+    g = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    inp, ph, bl, opts, thr, nsplit = dij_case(name, str(tmp_path / name))
+    prob = api.Problem.from_file(inp)
+    col, rows, vals, res = oracle.run_dij(prob, bl, rel_threshold=thr)
+    if platform.machine() == "x86_64":
+        np.testing.assert_array_equal(col, g["jc"])
+        np.testing.assert_array_equal(rows, g["ir"])
+        np.testing.assert_array_equal(vals, g["pr"])
+    else:
+        np.testing.assert_allclose(vals.sum(), g["pr"].sum(), rtol=1e-6)
+    assert res.histories == bl.n * opts["nHistories"]
+
+
+@pytest.mark.skipif(not __import__("oracle.binding", fromlist=["x"]).ref_matrad_available(),
+                    reason="reference matRad front end not built here")
+def test_live_reference_dij_with_uneven_options(oracle, native, tmp_path):
+    """Where the reference was built: a third beamlet set with other seeds
+    and a zero threshold, live against the reference."""
+    from ompmc_gb300 import api
+
+    inp, ph, bl, opts, thr, nsplit = dij_case("dij_slab", str(tmp_path / "live"), ncase=120, nbatch=4,
+                                              seeds=(12, 345))
+    opts["relDoseThreshold"] = 0.0
+    jc, ir, pr = oracle.ref_matrad(str(tmp_path / "live" / "ref"), ph, bl, opts)
+    prob = api.Problem.from_file(inp)
+    col, rows, vals, _ = oracle.run_dij(prob, bl, rel_threshold=0.0)
+    np.testing.assert_array_equal(col, jc)
+    np.testing.assert_array_equal(rows, ir)
+    np.testing.assert_array_equal(vals, pr)
