@@ -316,6 +316,64 @@ def run_ours(args, rank, world, local_rank, dist_on):
         return line
 
 
+DIJ_WORKLOAD = ("matRad-style dij: CT-like blob phantom 256x256x128 @ 2 mm, 7 gantry angles x 5 mm beamlets "
+                "within 3.5 cm of the axis, synthetic 6 MV, lognormal histories/beamlet (median 5e4, "
+                "sigma_ln 1.0, clipped [1e4, 1e6])")
+
+
+def run_dij_leg(args, local_rank):
+    """One batched dij job (every beamlet in one persistent launch per tally
+    group) on the CT-like phantom; histories/s of the transport and the
+    wall time of the whole call (transport, device compaction into CSC,
+    copy to host)."""
+    import torch
+
+    from ompmc_gb300 import api, data
+    from ompmc_gb300 import workloads as W
+
+    torch.cuda.set_device(local_rank)
+    data.stage()
+    P = data.paths()
+    with tempfile.TemporaryDirectory() as tmp:
+        ph = W.ct_like()
+        phantom = api.Phantom.from_arrays(ph.media, ph.xb, ph.yb, ph.zb, ph.med, ph.rho)
+        spec = W.write_spectrum(os.path.join(tmp, "6mv.spectrum"), "synthetic 6 MV", *W.spectrum_6mv())
+        job = W.Job("(in memory)", P["pegs"], P["pgs4form"], P["data_folder"], tmp + os.sep, spectrum_file=spec,
+                    ncase=50000, nbatch=1)
+        prob = api.Problem(api.Input(text=job.text()), phantom=phantom)
+        iso = (0.0, 0.0, 0.5 * (ph.zb[0] + ph.zb[-1]))
+        gantry = tuple(360.0 * k / 7 for k in range(7))
+        bl = W.beamlets(gantry_deg=gantry, iso=iso, sad=100.0, bixel=0.5, field=10.0, radius=3.5)
+        nh = W.lognormal_histories(bl.n, median=5e4, sigma=1.0, lo=1e4, hi=1e6, seed=7)
+        eng = api.Engine(local_rank).load(prob)
+        eng.set_beamlets(bl)
+        scale = args.dij_scale
+        nh = np.maximum(1, (nh * scale).astype(np.int64))
+        # warm-up on a 1/50 sample of every beamlet
+        eng.run_dij(rel_threshold=1e-4, nhist=np.maximum(1, nh // 50), precision=api.FP32, fp32_values=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        col, rows, vals, st = eng.run_dij(rel_threshold=1e-4, nhist=nh, precision=api.FP32, fp32_values=True,
+                                          seeds=(97, 33), continue_streams=1)
+        wall = time.perf_counter() - t0
+        if st.error_flags:
+            raise RuntimeError(f"device error flags {st.error_flags:#x}")
+        total = int(nh.sum())
+        line = {
+            "metric": "histories/s", "value": total / (st.kernel_ms / 1000.0), "unit": "histories/s", "n_gpus": 1,
+            "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": DIJ_WORKLOAD, "beamlets": bl.n, "histories": total,
+                       "transport": "FP32 arithmetic, FP64 tallies, FP32 dij values",
+                       "threshold": "1e-4 of each beamlet's max"},
+            "transport_s": st.kernel_ms / 1000.0, "wall_s": wall, "wall_histories_per_s": total / wall,
+            "nnz": int(len(vals)), "dij_bytes": int(len(vals) * 8 + len(col) * 8),
+            "per_history": {"events": st.steps / total, "voxel_steps": st.voxel_steps / total,
+                            "deposits": st.deposits / total},
+        }
+        eng.close()
+        return line
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -325,6 +383,8 @@ def main():
     ap.add_argument("--histories-per-step", type=int, default=HISTORIES_PER_STEP,
                     help="smaller values only for profiler captures of the same code path")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--dij", action="store_true", help="measure the batched dij workload instead (one JSON line)")
+    ap.add_argument("--dij-scale", type=float, default=1.0, help="scale of the dij history counts")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -333,6 +393,10 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference_arm(args, rank)
+        return
+    if args.dij:
+        if rank == 0:
+            print(json.dumps(run_dij_leg(args, local_rank)), flush=True)
         return
     dist_on = world > 1
     if dist_on:

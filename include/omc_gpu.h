@@ -417,6 +417,45 @@ omc_status omc_engine_run_dij(omc_engine *e, const omc_run_config *cfg,
                               const omc_dij_config *dcfg, omc_dij **out,
                               omc_run_stats *stats);
 
+/* ------------------------------------------------------------------------
+ * matRad entry point.  Replaces mexFunction of the omc_matrad front end
+ * (omc_matrad.c:1258-1530): the same five inputs as plain C data, the same
+ * sparse dij out.  A MATLAB binding wraps it in a few lines (mxGetPr of
+ * each field in, mxCreateSparse + copy out).
+ * ---------------------------------------------------------------------- */
+typedef struct omc_matrad_geo {
+    int nx, ny, nz;              /* size of cubeRho (x fastest)            */
+    const double *cube_rho;      /* cubeRho, [nx*ny*nz] g/cm^3             */
+    const int *cube_mat_ix;      /* cubeMatIx (int32), 1-based material    */
+    int nmaterials;              /* entries of mcGeo.material              */
+    const char *const *materials;/* mcGeo.material (pegs4 medium names)    */
+    const double *xbounds, *ybounds, *zbounds; /* mcGeo.x/y/zBounds (cm)   */
+} omc_matrad_geo;
+
+typedef struct omc_matrad_opt {  /* mcOpt (omc_matrad.c:62-250)            */
+    long long n_histories;       /* nHistories: histories per beamlet      */
+    int n_batches;               /* nBatches                               */
+    int n_split;                 /* nSplit                                 */
+    const char *spectrum_file;   /* spectrumFile; NULL or "" = monoEnergy
+                                    (the reference always reads a file)    */
+    double mono_energy;          /* monoEnergy (MeV)                       */
+    int charge;                  /* charge: read but not applied, the
+                                    reference's beams are always photons   */
+    double global_ecut, global_pcut;
+    int random_seeds[2];         /* randomSeeds                            */
+    const char *pegs_file, *pgs4form_file, *data_folder, *output_folder;
+    double rel_dose_threshold;   /* relDoseThreshold                       */
+    int verbose;                 /* verbose: progress lines on stdout      */
+} omc_matrad_opt;
+
+/* Builds tables, regions and source from the inputs, transports every
+ * beamlet on `device` (precision OMC_FP64 or OMC_FP32; serial = 1 runs the
+ * reference's serial order) and returns the dij in *out (free with
+ * omc_dij_free). */
+omc_status omc_matrad_dij(int device, const omc_matrad_geo *geo,
+                          const omc_beamlets *src, const omc_matrad_opt *opt,
+                          int precision, int serial, omc_dij **out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -88,6 +88,21 @@ class DijConfig_t(C.Structure):
                 ("tally_bytes", C.c_longlong)]
 
 
+class MatradGeo_t(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("cube_rho", C.POINTER(C.c_double)),
+                ("cube_mat_ix", C.POINTER(C.c_int)), ("nmaterials", C.c_int), ("materials", C.POINTER(C.c_char_p)),
+                ("xbounds", C.POINTER(C.c_double)), ("ybounds", C.POINTER(C.c_double)),
+                ("zbounds", C.POINTER(C.c_double))]
+
+
+class MatradOpt_t(C.Structure):
+    _fields_ = [("n_histories", C.c_longlong), ("n_batches", C.c_int), ("n_split", C.c_int),
+                ("spectrum_file", C.c_char_p), ("mono_energy", C.c_double), ("charge", C.c_int),
+                ("global_ecut", C.c_double), ("global_pcut", C.c_double), ("random_seeds", C.c_int * 2),
+                ("pegs_file", C.c_char_p), ("pgs4form_file", C.c_char_p), ("data_folder", C.c_char_p),
+                ("output_folder", C.c_char_p), ("rel_dose_threshold", C.c_double), ("verbose", C.c_int)]
+
+
 _lib = None
 
 
@@ -135,6 +150,8 @@ def lib(path: str | None = None):
         "omc_engine_set_beamlets": ([vp, pp(Beamlets_t)], C.c_int),
         "omc_engine_run_dij": ([vp, pp(RunConfig_t), pp(DijConfig_t), pp(pp(Dij_t)), pp(RunStats_t)], C.c_int),
         "omc_dij_free": ([pp(Dij_t)], None),
+        "omc_matrad_dij": ([C.c_int, pp(MatradGeo_t), pp(Beamlets_t), pp(MatradOpt_t), C.c_int, C.c_int,
+                            pp(pp(Dij_t))], C.c_int),
         "omc_gpu_ranmar": ([C.c_int, C.c_int, C.c_int, C.c_int, C.c_longlong, pp(C.c_int32)], C.c_int),
         "omc_stream_seeds": ([C.c_int, C.c_int, C.c_longlong, pp(C.c_int), pp(C.c_int)], None),
     }

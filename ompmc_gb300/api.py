@@ -221,17 +221,9 @@ class Engine:
     def set_beamlets(self, beamlets):
         """Upload a :class:`ompmc_gb300.workloads.Beamlets` set (the
         matRad mcSrc fields)."""
-        b = beamlets
-        keep = [np.ascontiguousarray(b.ibeam, dtype=np.int32)]
-        cols = []
-        for arr in (b.source[:, 0], b.source[:, 1], b.source[:, 2], b.corner[:, 0], b.corner[:, 1], b.corner[:, 2],
-                    b.side1[:, 0], b.side1[:, 1], b.side1[:, 2], b.side2[:, 0], b.side2[:, 1], b.side2[:, 2]):
-            a = np.ascontiguousarray(arr, dtype=np.float64)
-            keep.append(a)
-            cols.append(_dptr(a))
-        st = N.Beamlets_t(len(b.ibeam), len(b.source), keep[0].ctypes.data_as(C.POINTER(C.c_int)), *cols)
+        st, keep = _beamlets_t(beamlets)
         check(N.lib().omc_engine_set_beamlets(self._h, C.byref(st)))
-        self._beamlets = b
+        self._beamlets = beamlets
         return self
 
     def run_dij(self, rel_threshold=1e-4, nhist=None, nperbatch=None, nbatch=None, seeds=None, nsplit=None,
@@ -252,18 +244,7 @@ class Engine:
         out = C.POINTER(N.Dij_t)()
         st = N.RunStats_t()
         check(N.lib().omc_engine_run_dij(self._h, C.byref(cfg), C.byref(dc), C.byref(out), C.byref(st)))
-        try:
-            d = out.contents
-            col_ptr = np.ctypeslib.as_array(d.col_ptr, shape=(d.ncols + 1,)).copy()
-            if d.nnz:
-                rows = np.ctypeslib.as_array(d.row_idx, shape=(d.nnz,)).copy()
-                vp = d.values_f32 if fp32_values else d.values
-                vals = np.ctypeslib.as_array(vp, shape=(d.nnz,)).copy()
-            else:
-                rows = np.zeros(0, np.int32)
-                vals = np.zeros(0, np.float32 if fp32_values else np.float64)
-        finally:
-            N.lib().omc_dij_free(out)
+        col_ptr, rows, vals = _take_dij(out, fp32_values)
         return col_ptr, rows, vals, st
 
     def close(self):
@@ -273,6 +254,58 @@ class Engine:
 
     def __del__(self):
         self.close()
+
+
+def _beamlets_t(b):
+    keep = [np.ascontiguousarray(b.ibeam, dtype=np.int32)]
+    cols = []
+    for arr in (b.source[:, 0], b.source[:, 1], b.source[:, 2], b.corner[:, 0], b.corner[:, 1], b.corner[:, 2],
+                b.side1[:, 0], b.side1[:, 1], b.side1[:, 2], b.side2[:, 0], b.side2[:, 1], b.side2[:, 2]):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        keep.append(a)
+        cols.append(_dptr(a))
+    return N.Beamlets_t(len(b.ibeam), len(b.source), keep[0].ctypes.data_as(C.POINTER(C.c_int)), *cols), keep
+
+
+def _take_dij(out, fp32=False):
+    try:
+        d = out.contents
+        col = np.ctypeslib.as_array(d.col_ptr, shape=(d.ncols + 1,)).copy()
+        if d.nnz:
+            rows = np.ctypeslib.as_array(d.row_idx, shape=(d.nnz,)).copy()
+            vals = np.ctypeslib.as_array(d.values_f32 if fp32 else d.values, shape=(d.nnz,)).copy()
+        else:
+            rows, vals = np.zeros(0, np.int32), np.zeros(0, np.float32 if fp32 else np.float64)
+    finally:
+        N.lib().omc_dij_free(out)
+    return col, rows, vals
+
+
+def matrad_dij(phantom, beamlets, opts, precision=FP64, serial=0, device=0):
+    """omc_matrad_dij: matRad's five inputs (cube from a
+    :class:`ompmc_gb300.workloads.Phantom`, mcSrc from a
+    :class:`ompmc_gb300.workloads.Beamlets`, mcOpt fields as a dict with
+    matRad's names) in, (col_ptr, row_idx, values) out."""
+    nz, ny, nx = phantom.shape
+    rho = np.ascontiguousarray(phantom.rho, dtype=np.float64)
+    mix = np.ascontiguousarray(phantom.med, dtype=np.int32)
+    names = (C.c_char_p * len(phantom.media))(*[m.encode() for m in phantom.media])
+    xb, yb, zb = (np.ascontiguousarray(b, dtype=np.float64) for b in (phantom.xb, phantom.yb, phantom.zb))
+    geo = N.MatradGeo_t(nx, ny, nz, _dptr(rho), mix.ctypes.data_as(C.POINTER(C.c_int)), len(phantom.media), names,
+                        _dptr(xb), _dptr(yb), _dptr(zb))
+    enc = lambda k: opts[k].encode() if opts.get(k) else None
+    seeds = (C.c_int * 2)(*[int(x) for x in opts.get("randomSeeds", (97, 33))])
+    opt = N.MatradOpt_t(int(opts["nHistories"]), int(opts["nBatches"]), int(opts.get("nSplit", 1)),
+                        enc("spectrumFile"), float(opts.get("monoEnergy", 0.0)), int(opts.get("charge", 0)),
+                        float(opts["global_ecut"]), float(opts["global_pcut"]), seeds, enc("pegsFile"),
+                        enc("pgs4formFile"), enc("dataFolder"), enc("outputFolder"),
+                        float(opts["relDoseThreshold"]), int(bool(opts.get("verbose", 0))))
+    bl, keep = _beamlets_t(beamlets)
+    out = C.POINTER(N.Dij_t)()
+    check(N.lib().omc_matrad_dij(device, C.byref(geo), C.byref(bl), C.byref(opt), precision, serial,
+                                 C.byref(out)))
+    del keep
+    return _take_dij(out)
 
 
 def gpu_ranmar(ixx, jxx, nstreams, n, device=0):
