@@ -374,6 +374,95 @@ def run_dij_leg(args, local_rank):
         return line
 
 
+SERVE_WORKLOAD = ("dose-server mix: Poisson arrivals; phantom homogeneous water / z-slab / seeded blob at 64^3, "
+                  "128^3 or 256x256x160 (2-4.7 mm voxels over a 30-48 cm box); source 1.25 MeV, synthetic 6 MV or "
+                  "synthetic 250 kVp, 10x10 cm2 field at SSD 100 cm; histories log-uniform over [1e5, 1e8]; "
+                  "10 batches per job")
+
+
+def serve_library():
+    """Phantoms of the serving mix (generated once) and the three sources."""
+    from ompmc_gb300 import workloads as W
+
+    sizes = [(64, 64, 64, 0.469), (128, 128, 128, 0.234), (256, 256, 160, 0.1875)]
+    phantoms = []
+    for nx, ny, nz, vox in sizes:
+        phantoms.append(("water", W.homogeneous(vox=vox, nxyz=(nx, ny, nz))))
+        layers = ((0.0, 5.0, W.WATER, 1.0), (5.0, 15.0, W.LUNG, 0.26), (15.0, 18.0, W.BONE, 1.85),
+                  (18.0, nz * vox + 1.0, W.WATER, 1.0))
+        sl = W.slab(vox=vox, layers=layers, nxyz=(nx, ny, nz))
+        phantoms.append(("slab", sl))
+        phantoms.append(("blob", W.ct_like(nx=nx, ny=ny, nz=nz, vox=vox, seed=11 + nx)))
+    return phantoms
+
+
+def run_serve_leg(args, local_rank):
+    import torch
+
+    from ompmc_gb300 import api, data
+    from ompmc_gb300 import workloads as W
+
+    torch.cuda.set_device(local_rank)
+    data.stage()
+    P = data.paths()
+    rng = np.random.default_rng(args.serve_seed)
+    with tempfile.TemporaryDirectory() as tmp:
+        lib = serve_library()
+        phs = [api.Phantom.from_arrays(p.media, p.xb, p.yb, p.zb, p.med, p.rho) for _, p in lib]
+        spec6 = W.write_spectrum(os.path.join(tmp, "6mv.spectrum"), "synthetic 6 MV", *W.spectrum_6mv())
+        spec250 = W.write_spectrum(os.path.join(tmp, "250.spectrum"), "synthetic 250 kVp", *W.spectrum_250kvp())
+        texts = []
+        for spec in (None, spec6, spec250):
+            job = W.Job("(in memory)", P["pegs"], P["pgs4form"], P["data_folder"], tmp + os.sep,
+                        spectrum_file=spec, mono_energy=1.25, collimator=(-5.0, 5.0, -5.0, 5.0), ssd=100.0)
+            texts.append(job.text())
+        inputs = [api.Input(text=t) for t in texts]
+        sources = {}
+        njobs = args.serve_jobs
+        draws = []
+        for _ in range(njobs):
+            ip = int(rng.integers(len(phs)))
+            isrc = int(rng.integers(3))
+            nh = int(10 ** rng.uniform(5.0, np.log10(args.serve_max_histories)))
+            nh -= nh % 10
+            draws.append((ip, isrc, max(nh, 10)))
+            if (ip, isrc) not in sources:
+                sources[(ip, isrc)] = api.build_source(inputs[isrc], phs[ip])
+        mean_h = float(np.mean([d[2] for d in draws]))
+        gaps = rng.exponential(1.0 / args.serve_rate, size=njobs)
+        media = [W.AIR, W.LUNG, W.WATER, W.BONE]
+        data_text = f"pegs file = {P['pegs']}\npgs4form file = {P['pgs4form']}\ndata folder = {P['data_folder']}\n"
+        out = {}
+        for mode, max_jobs in (("continuous", 0), ("one_at_a_time", 1)):
+            srv = api.Server(media, data_text, precision=api.FP32, max_jobs=max_jobs)
+            # warm-up job (tables, kernels)
+            srv.wait(srv.submit(phs[0], sources.get((0, 0)) or api.build_source(inputs[0], phs[0]), 0.7, 0.01,
+                                1000, 10))
+            ids = []
+            t0 = time.perf_counter()
+            for (ip, isrc, nh), gap in zip(draws, gaps):
+                time.sleep(gap)
+                ids.append(srv.submit(phs[ip], sources[(ip, isrc)], 0.7, 0.01, nh // 10, 10))
+            res = [srv.wait(i)[2] for i in ids]
+            makespan = time.perf_counter() - t0
+            st = srv.stats()
+            srv.close()
+            lat = np.array([r.finish_s - r.submit_s for r in res])
+            tot = sum(d[2] for d in draws)
+            out[mode] = {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+                         "mean_s": float(lat.mean()), "histories_per_s": tot / makespan,
+                         "gpu_transport_s": st.transport_s, "rounds": int(st.rounds),
+                         "max_resident": int(st.max_resident), "max_round_jobs": int(st.max_round_jobs)}
+        for src in sources.values():
+            api.free_source(src)
+        total = sum(d[2] for d in draws)
+        return {"metric": "job latency p50/p99 (s) and histories/s", "n_gpus": 1, "data": "synthetic",
+                "dtype": "f32", "config": {"workload": SERVE_WORKLOAD, "jobs": njobs, "rate_per_s": args.serve_rate,
+                                           "mean_histories": mean_h, "total_histories": total,
+                                           "seed": args.serve_seed},
+                "continuous": out["continuous"], "one_at_a_time": out["one_at_a_time"]}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -385,6 +474,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--dij", action="store_true", help="measure the batched dij workload instead (one JSON line)")
     ap.add_argument("--dij-scale", type=float, default=1.0, help="scale of the dij history counts")
+    ap.add_argument("--serve", action="store_true", help="measure the dose-server mix instead (one JSON line)")
+    ap.add_argument("--serve-jobs", type=int, default=40)
+    ap.add_argument("--serve-rate", type=float, default=0.5, help="job arrivals per second")
+    ap.add_argument("--serve-max-histories", type=float, default=1e8)
+    ap.add_argument("--serve-seed", type=int, default=5)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -397,6 +491,10 @@ def main():
     if args.dij:
         if rank == 0:
             print(json.dumps(run_dij_leg(args, local_rank)), flush=True)
+        return
+    if args.serve:
+        if rank == 0:
+            print(json.dumps(run_serve_leg(args, local_rank)), flush=True)
         return
     dist_on = world > 1
     if dist_on:

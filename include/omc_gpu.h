@@ -339,6 +339,9 @@ omc_status omc_engine_run_resident(omc_engine *e, const omc_run_config *cfg,
 omc_status omc_engine_run_noalloc(omc_engine *e, const omc_run_config *cfg,
                                   double *d_endep, omc_run_stats *stats);
 
+/* Free and total device memory of a CUDA device (bytes). */
+omc_status omc_device_memory(int device, size_t *free_bytes, size_t *total_bytes);
+
 /* RANMAR streams on the device (bit-exact with initRandom/setRandom,
  * omc_random.c:58-187).  Stream k is seeded with the k-th pair of the
  * sequence (ixx, jxx), (ixx, jxx+1), ..., (the reference's per-thread
@@ -416,6 +419,115 @@ typedef struct omc_dij_config {
 omc_status omc_engine_run_dij(omc_engine *e, const omc_run_config *cfg,
                               const omc_dij_config *dcfg, omc_dij **out,
                               omc_run_stats *stats);
+
+/* ------------------------------------------------------------------------
+ * Resident dose jobs.  Several omc_dosxyz-style jobs (own phantom, source,
+ * cuts, batches) stay on one engine and share its tables; a round
+ * transports the next quota[i] histories of every jobs[i] in ONE launch,
+ * their particles in flight together.  History k of a job (counted over
+ * rounds) scores in batch k / nperbatch, so a finished job returns the
+ * same batch sums as omc_engine_run.  The regions of a job must be built
+ * with the engine's tables (same media in the same order).  No
+ * counterpart in the reference, which runs one job per process; this is
+ * the layer the dose server (omc_server_*) schedules.
+ * ---------------------------------------------------------------------- */
+typedef struct omc_job omc_job;
+
+/* Device bytes a job of this phantom holds while resident. */
+size_t omc_job_device_bytes(const omc_phantom *ph, int nbatch, int precision);
+
+omc_status omc_engine_job_add(omc_engine *e, const omc_phantom *ph,
+                              const omc_regions *r, const omc_source *src,
+                              long long nperbatch, int nbatch, int precision,
+                              omc_job **out);
+/* Histories transported so far / in total. */
+long long omc_job_done(const omc_job *j);
+long long omc_job_histories(const omc_job *j);
+/* One launch over njobs jobs of one precision.  cfg supplies nsplit,
+ * inflight and the seeds used when the streams are (re)seeded: streams
+ * continue between rounds when cfg->continue_streams is set. */
+omc_status omc_engine_job_round(omc_engine *e, omc_job *const *jobs,
+                                const long long *quota, int njobs,
+                                const omc_run_config *cfg,
+                                omc_run_stats *stats);
+/* Batch sums (score.accum_endep / accum_endep2, nreg entries each, may be
+ * NULL) and source energy of the histories transported so far. */
+omc_status omc_engine_job_result(omc_engine *e, omc_job *j,
+                                 double *accum_endep, double *accum_endep2,
+                                 double *ensrc);
+void omc_engine_job_remove(omc_engine *e, omc_job *j);
+
+/* ------------------------------------------------------------------------
+ * Dose server: continuous batching of dose jobs on one GPU.  Jobs are
+ * submitted from any thread and queue in arrival order; an admission
+ * thread moves the head job onto the device (phantom, source, tallies) as
+ * soon as the device-memory budget and the job limit allow, overlapping
+ * its upload with transport; a scheduler thread runs rounds: one launch in
+ * which every resident job advances by its share of round_histories
+ * histories, so jobs that arrive while others run join at the next round
+ * and small jobs finish without waiting for large ones.  Finished jobs
+ * leave the device at once.  No counterpart in the reference.
+ * ---------------------------------------------------------------------- */
+typedef struct omc_server omc_server;
+
+typedef struct omc_server_config {
+    int device;
+    int precision;              /* OMC_FP32 or OMC_FP64, for every job     */
+    long long hbm_budget;       /* device bytes for resident jobs; 0 = half
+                                   the free memory at creation            */
+    int max_jobs;               /* resident jobs at most; 0 = 256          */
+    long long round_histories;  /* histories per round over all resident
+                                   jobs; 0 = 4,000,000                     */
+    int nsplit;                 /* photon splitting, every job (0 = 1)     */
+    int ixx, jxx;               /* RANMAR seeds of the server's streams    */
+} omc_server_config;
+
+/* The server's media: every job's phantom media must be among them.
+ * data_keys supplies "pegs file", "pgs4form file" and "data folder"; the
+ * tables are built once and stay resident. */
+omc_status omc_server_create(const omc_server_config *cfg,
+                             const omc_input *data_keys, int nmed,
+                             const char *const *media, omc_server **out);
+
+typedef struct omc_server_job {
+    const omc_phantom *phantom; /* copied by submit                        */
+    const omc_source *source;   /* copied by submit                        */
+    double ecut, pcut;          /* "global ecut" / "global pcut" (MeV)     */
+    long long nperbatch;
+    int nbatch;
+} omc_server_job;
+
+omc_status omc_server_submit(omc_server *s, const omc_server_job *job,
+                             long long *id);
+
+typedef struct omc_server_result {
+    double ensrc;               /* source kinetic energy (MeV)             */
+    long long histories;
+    double submit_s;            /* times since omc_server_create (s)       */
+    double admit_s;             /* resident on the device                  */
+    double finish_s;            /* tallies back on the host                */
+    int rounds;                 /* rounds the job took part in             */
+    int status;                 /* omc_status of the job                   */
+} omc_server_result;
+
+/* Waits for job id (timeout_s < 0: without limit; OMC_ERR_LIMIT on
+ * timeout, the job stays queued), copies its batch sums (nreg entries
+ * each, may be NULL) and forgets the job. */
+omc_status omc_server_wait(omc_server *s, long long id, double timeout_s,
+                           double *accum_endep, double *accum_endep2,
+                           omc_server_result *res);
+
+typedef struct omc_server_stats {
+    long long submitted, finished, rounds, histories;
+    int max_resident;           /* most jobs resident at once              */
+    int max_round_jobs;         /* most jobs in one round                  */
+    long long max_resident_bytes;
+    double transport_s;         /* device time of all rounds               */
+} omc_server_stats;
+
+omc_status omc_server_get_stats(omc_server *s, omc_server_stats *st);
+/* Stops both threads after the current round; queued jobs are dropped. */
+void omc_server_destroy(omc_server *s);
 
 /* ------------------------------------------------------------------------
  * matRad entry point.  Replaces mexFunction of the omc_matrad front end

@@ -103,6 +103,27 @@ class MatradOpt_t(C.Structure):
                 ("output_folder", C.c_char_p), ("rel_dose_threshold", C.c_double), ("verbose", C.c_int)]
 
 
+class ServerConfig_t(C.Structure):
+    _fields_ = [("device", C.c_int), ("precision", C.c_int), ("hbm_budget", C.c_longlong), ("max_jobs", C.c_int),
+                ("round_histories", C.c_longlong), ("nsplit", C.c_int), ("ixx", C.c_int), ("jxx", C.c_int)]
+
+
+class ServerJob_t(C.Structure):
+    _fields_ = [("phantom", C.POINTER(Phantom_t)), ("source", C.POINTER(Source_t)), ("ecut", C.c_double),
+                ("pcut", C.c_double), ("nperbatch", C.c_longlong), ("nbatch", C.c_int)]
+
+
+class ServerResult_t(C.Structure):
+    _fields_ = [("ensrc", C.c_double), ("histories", C.c_longlong), ("submit_s", C.c_double),
+                ("admit_s", C.c_double), ("finish_s", C.c_double), ("rounds", C.c_int), ("status", C.c_int)]
+
+
+class ServerStats_t(C.Structure):
+    _fields_ = [("submitted", C.c_longlong), ("finished", C.c_longlong), ("rounds", C.c_longlong),
+                ("histories", C.c_longlong), ("max_resident", C.c_int), ("max_round_jobs", C.c_int),
+                ("max_resident_bytes", C.c_longlong), ("transport_s", C.c_double)]
+
+
 _lib = None
 
 
@@ -152,6 +173,22 @@ def lib(path: str | None = None):
         "omc_dij_free": ([pp(Dij_t)], None),
         "omc_matrad_dij": ([C.c_int, pp(MatradGeo_t), pp(Beamlets_t), pp(MatradOpt_t), C.c_int, C.c_int,
                             pp(pp(Dij_t))], C.c_int),
+        "omc_job_device_bytes": ([pp(Phantom_t), C.c_int, C.c_int], C.c_size_t),
+        "omc_engine_job_add": ([vp, pp(Phantom_t), pp(Regions_t), pp(Source_t), C.c_longlong, C.c_int, C.c_int,
+                                pp(vp)], C.c_int),
+        "omc_job_done": ([vp], C.c_longlong),
+        "omc_job_histories": ([vp], C.c_longlong),
+        "omc_engine_job_round": ([vp, pp(vp), pp(C.c_longlong), C.c_int, pp(RunConfig_t), pp(RunStats_t)],
+                                 C.c_int),
+        "omc_engine_job_result": ([vp, vp, pp(C.c_double), pp(C.c_double), pp(C.c_double)], C.c_int),
+        "omc_engine_job_remove": ([vp, vp], None),
+        "omc_server_create": ([pp(ServerConfig_t), vp, C.c_int, pp(C.c_char_p), pp(vp)], C.c_int),
+        "omc_server_submit": ([vp, pp(ServerJob_t), pp(C.c_longlong)], C.c_int),
+        "omc_server_wait": ([vp, C.c_longlong, C.c_double, pp(C.c_double), pp(C.c_double), pp(ServerResult_t)],
+                            C.c_int),
+        "omc_server_get_stats": ([vp, pp(ServerStats_t)], C.c_int),
+        "omc_server_destroy": ([vp], None),
+        "omc_device_memory": ([C.c_int, pp(C.c_size_t), pp(C.c_size_t)], C.c_int),
         "omc_gpu_ranmar": ([C.c_int, C.c_int, C.c_int, C.c_int, C.c_longlong, pp(C.c_int32)], C.c_int),
         "omc_stream_seeds": ([C.c_int, C.c_int, C.c_longlong, pp(C.c_int), pp(C.c_int)], None),
     }

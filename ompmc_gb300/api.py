@@ -102,6 +102,18 @@ class Phantom:
             self._p = None
 
 
+def build_source(inp: "Input", phantom: "Phantom"):
+    """omc_source_build (initSource) alone: POINTER(Source_t), free with
+    free_source."""
+    src = C.POINTER(N.Source_t)()
+    check(N.lib().omc_source_build(inp._h, phantom._p, C.byref(src)))
+    return src
+
+
+def free_source(src):
+    N.lib().omc_source_free(src)
+
+
 class Problem:
     """Host-side state of one dose job, built from a .inp file."""
 
@@ -250,6 +262,59 @@ class Engine:
     def close(self):
         if getattr(self, "_h", None):
             N.lib().omc_engine_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+class Server:
+    """Dose server (omc_server_*): continuous batching of dose jobs on one
+    GPU.  `media` are the server's pegs4 media; `data_text` is .inp text
+    with the "pegs file", "pgs4form file" and "data folder" keys."""
+
+    def __init__(self, media, data_text, precision=FP32, hbm_budget=0, max_jobs=0, round_histories=0, nsplit=1,
+                 seeds=(97, 33), device=0):
+        self._inp = Input(text=data_text)
+        cfg = N.ServerConfig_t(device, precision, int(hbm_budget), int(max_jobs), int(round_histories),
+                               int(nsplit), int(seeds[0]), int(seeds[1]))
+        names = (C.c_char_p * len(media))(*[m.encode() for m in media])
+        self._h = C.c_void_p()
+        check(N.lib().omc_server_create(C.byref(cfg), self._inp._h, len(media), names, C.byref(self._h)))
+        self._nreg = {}
+
+    def submit(self, phantom, source, ecut, pcut, nperbatch, nbatch):
+        """phantom: :class:`Phantom`; source: a POINTER(Source_t) (e.g.
+        Problem.source).  Returns the job id."""
+        job = N.ServerJob_t(phantom._p, source, float(ecut), float(pcut), int(nperbatch), int(nbatch))
+        jid = C.c_longlong()
+        check(N.lib().omc_server_submit(self._h, C.byref(job), C.byref(jid)))
+        self._nreg[jid.value] = phantom.nreg
+        return jid.value
+
+    def submit_problem(self, prob, nperbatch=None, nbatch=None):
+        g = lambda k: float(prob.input.get(k))
+        return self.submit(prob.phantom, prob.source, g("global ecut"), g("global pcut"),
+                           prob.nperbatch if nperbatch is None else nperbatch,
+                           prob.nbatch if nbatch is None else nbatch)
+
+    def wait(self, jid, timeout=-1.0):
+        """(accum_endep, accum_endep2, ServerResult_t) of a finished job."""
+        nreg = self._nreg.pop(jid)
+        a = np.zeros(nreg)
+        a2 = np.zeros(nreg)
+        r = N.ServerResult_t()
+        check(N.lib().omc_server_wait(self._h, jid, float(timeout), _dptr(a), _dptr(a2), C.byref(r)))
+        return a, a2, r
+
+    def stats(self):
+        st = N.ServerStats_t()
+        check(N.lib().omc_server_get_stats(self._h, C.byref(st)))
+        return st
+
+    def close(self):
+        if getattr(self, "_h", None):
+            N.lib().omc_server_destroy(self._h)
             self._h = None
 
     def __del__(self):

@@ -120,6 +120,23 @@ struct Source {
   const int *ibeam;    // [nbeamlets]
 };
 
+// One resident dose job of a multi-job launch: its own phantom, source,
+// per-batch tallies and source-energy sum.  History k of the job (counted
+// over all launches) belongs to batch k / nperbatch.
+template <typename R>
+struct JobSlot {
+  Geometry<R> G;
+  Source<R> S;
+  double *tally;        // [nbatch][nreg]
+  double *ensrc;        // [1]
+  long long nreg;
+  long long h0;         // job history index of this launch's first history
+  long long nperbatch;
+};
+
+// Queue tag of a particle in a multi-job launch: job slot and batch.
+constexpr int kBatchTag = 4096;
+
 template <typename R>
 struct Params {
   Tables<R> T;
@@ -142,6 +159,7 @@ struct Params {
   const long long *slot_first;       // [nslots+1]
   const int *slot_beamlet;           // [nslots]
   long long tally_stride;            // nreg
+  const JobSlot<R> *__restrict__ jobs;  // multi-job launches: [nslots]
   // outputs
   double *endep;             // [nreg] batch tally ([nslots][nreg] with slots)
   double *ensrc;             // [1]

@@ -14,6 +14,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -197,7 +198,7 @@ __device__ bool grid_barrier(unsigned *arrive, unsigned *gen, unsigned nblocks) 
 
 __device__ __forceinline__ unsigned vload(const unsigned *p) { return *static_cast<const volatile unsigned *>(p); }
 
-template <typename R>
+template <typename R, bool MULTI>
 __global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) wavefront_kernel(Params<R> P, Wavefront<R> W) {
   extern __shared__ unsigned char s_raw[];
   const int t = threadIdx.x;
@@ -205,7 +206,7 @@ __global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) wavefront_ke
   const int lane_id = t & 31;
   RngPlanes sp = rng_planes(s_raw);
   rng_to_smem(P.rng_u, P.nlanes, gtid, sp, t);
-  Lane<R, true> L(P, gtid, sp.lo + t, sp.hi + t, kBlock);
+  Lane<R, true, MULTI> L(P, gtid, sp.lo + t, sp.hi + t, kBlock);
   L.rng.i = P.rng_ijc[gtid];
   L.rng.j = P.rng_ijc[P.nlanes + gtid];
   L.rng.c = P.rng_ijc[2 * P.nlanes + gtid];
@@ -518,9 +519,10 @@ struct PrecisionState {
 struct SlotJob {
   int nslots;
   const long long *first;  // device [nslots+1]
-  const int *beamlet;      // device [nslots]
-  double *tally;           // device [nslots][nreg]
+  const int *beamlet;      // device [nslots] (beamlet jobs), else null
+  double *tally;           // device [nslots][nreg] (beamlet jobs), else null
   long long nhist;         // histories of the launch
+  const void *jobs;        // device JobSlot<R>[nslots] (multi-job launches), else null
 };
 
 }  // namespace
@@ -543,6 +545,8 @@ struct omc_engine {
   int nbeamlets = 0, nbeams = 0;
   // beamlet-job buffers
   DevBuf dij_tally, dij_first, dij_beamlet, dij_nhist, dij_max, dij_cnt, dij_off, dij_rows, dij_vals;
+  // multi-job rounds
+  DevBuf multi_slots, multi_first;
   // host copies needed across uploads
   omc_tables host_tables_dims{};
 };
@@ -752,9 +756,14 @@ void apply_job(Params<R> &P, const PrecisionState<R> &S, const SlotJob *job, lon
   if (!job) return;
   P.nslots = job->nslots;
   P.slot_first = job->first;
+  P.nhist = job->nhist;
+  if (job->jobs) {
+    P.jobs = static_cast<const JobSlot<R> *>(job->jobs);
+    P.endep = nullptr;
+    return;
+  }
   P.slot_beamlet = job->beamlet;
   P.endep = job->tally;
-  P.nhist = job->nhist;
   P.S.beamlets = 1;
   P.S.bixel = S.bixel;
   P.S.beam_src = S.beam_src;
@@ -869,12 +878,13 @@ struct WfCounters {
   unsigned hwm;
 };
 
-template <typename R>
+template <typename R, bool MULTI = false>
 int wavefront_blocks(omc_engine *e) {
   size_t smem = kRngSmem;
-  cudaFuncSetAttribute(wavefront_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  cudaFuncSetAttribute(wavefront_kernel<R, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       static_cast<int>(smem));
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wavefront_kernel<R>, kBlock, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wavefront_kernel<R, MULTI>, kBlock, smem);
   return (per_sm < 1 ? 1 : per_sm) * e->nsm;
 }
 
@@ -950,8 +960,9 @@ omc_status run_wavefront(omc_engine *e, PrecisionState<R> &S, const omc_run_conf
   for (int b = 0; b < nlaunch && err == cudaSuccess; b++) {
     cudaMemsetAsync(wc, 0, sizeof(WfCounters), e->stream);
     void *args[] = {&P, &W};
-    err = cudaLaunchCooperativeKernel(reinterpret_cast<void *>(wavefront_kernel<R>), dim3(blocks), dim3(kBlock),
-                                      args, smem, e->stream);
+    void *fn = (job && job->jobs) ? reinterpret_cast<void *>(wavefront_kernel<R, true>)
+                                  : reinterpret_cast<void *>(wavefront_kernel<R, false>);
+    err = cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(kBlock), args, smem, e->stream);
     if (job) continue;
     accumulate_kernel<<<std::max(1, std::min(4 * e->nsm, (e->nreg + 255) / 256)), 256, 0, e->stream>>>(
         static_cast<double *>(e->endep.p), static_cast<double *>(e->acc.p), static_cast<double *>(e->acc2.p),
@@ -1055,7 +1066,7 @@ extern "C" void omc_engine_destroy(omc_engine *e) {
   e->f64.beamlets.clear();
   e->f32.beamlets.clear();
   for (DevBuf *b : {&e->dij_tally, &e->dij_first, &e->dij_beamlet, &e->dij_nhist, &e->dij_max, &e->dij_cnt,
-                    &e->dij_off, &e->dij_rows, &e->dij_vals})
+                    &e->dij_off, &e->dij_rows, &e->dij_vals, &e->multi_slots, &e->multi_first})
     b->release();
   cudaStreamDestroy(e->stream);
   delete e;
@@ -1071,34 +1082,54 @@ extern "C" omc_status omc_engine_set_tables(omc_engine *e, const omc_tables *t) 
   return OMC_OK;
 }
 
+namespace {
+
+// Per-region medium, density ratio and per-medium cuts in the device
+// layout.  ecut/pcut are per region in the reference; initRegions makes
+// them a function of the medium, which is what the device stores.
+struct RegionData {
+  std::vector<int8_t> med;
+  std::vector<double> rhof, ecut_m, pcut_m;
+};
+
+omc_status region_data(int nmed, const omc_phantom *ph, const omc_regions *r, RegionData &d) {
+  int nreg = ph->nx * ph->ny * ph->nz + 1;
+  if (r->nreg != nreg) return fail(OMC_ERR_ARG, "regions (%d) do not match the phantom (%d)", r->nreg, nreg);
+  d.med.assign(nreg, 0);
+  d.rhof.assign(r->rhof, r->rhof + nreg);
+  d.ecut_m.assign(nmed + 1, 0.0);
+  d.pcut_m.assign(nmed + 1, 0.0);
+  std::vector<int> seen(nmed + 1, 0);
+  for (int i = 0; i < nreg; i++) {
+    int m = r->med[i];
+    if (m < -1 || m >= nmed) return fail(OMC_ERR_ARG, "region %d: medium %d outside -1..%d", i, m, nmed - 1);
+    d.med[i] = static_cast<int8_t>(m);
+    if (i == 0) continue;
+    if (!seen[m + 1]) {
+      d.ecut_m[m + 1] = r->ecut[i];
+      d.pcut_m[m + 1] = r->pcut[i];
+      seen[m + 1] = 1;
+    } else if (d.ecut_m[m + 1] != r->ecut[i] || d.pcut_m[m + 1] != r->pcut[i]) {
+      return fail(OMC_ERR_ARG, "region %d: ecut/pcut differ within medium %d", i, m);
+    }
+  }
+  d.ecut_m[0] = 0.0;
+  d.pcut_m[0] = 0.0;
+  return OMC_OK;
+}
+
+}  // namespace
+
 extern "C" omc_status omc_engine_set_geometry(omc_engine *e, const omc_phantom *ph, const omc_regions *r) {
   if (!e || !ph || !r) return fail(OMC_ERR_ARG, "null argument");
   if (!e->f64.tables_ok) return fail(OMC_ERR_STATE, "omc_engine_set_tables must come first");
   int nmed = e->host_tables_dims.nmed;
   int nreg = ph->nx * ph->ny * ph->nz + 1;
-  if (r->nreg != nreg) return fail(OMC_ERR_ARG, "regions (%d) do not match the phantom (%d)", r->nreg, nreg);
-  std::vector<int8_t> med(nreg);
-  std::vector<double> rhof(r->rhof, r->rhof + nreg);
-  // ecut/pcut are per region in the reference; initRegions makes them a
-  // function of the medium, which is what the device stores.
-  std::vector<double> ecut_m(nmed + 1, 0.0), pcut_m(nmed + 1, 0.0);
-  std::vector<int> seen(nmed + 1, 0);
-  for (int i = 0; i < nreg; i++) {
-    int m = r->med[i];
-    if (m < -1 || m >= nmed) return fail(OMC_ERR_ARG, "region %d: medium %d outside -1..%d", i, m, nmed - 1);
-    med[i] = static_cast<int8_t>(m);
-    if (i == 0) continue;
-    if (!seen[m + 1]) {
-      ecut_m[m + 1] = r->ecut[i];
-      pcut_m[m + 1] = r->pcut[i];
-      seen[m + 1] = 1;
-    } else if (ecut_m[m + 1] != r->ecut[i] || pcut_m[m + 1] != r->pcut[i]) {
-      return fail(OMC_ERR_ARG, "region %d: ecut/pcut differ within medium %d", i, m);
-    }
-  }
-  ecut_m[0] = 0.0;
-  pcut_m[0] = 0.0;
+  RegionData rd;
   omc_status s;
+  if ((s = region_data(nmed, ph, r, rd)) != OMC_OK) return s;
+  const std::vector<int8_t> &med = rd.med;
+  const std::vector<double> &rhof = rd.rhof, &ecut_m = rd.ecut_m, &pcut_m = rd.pcut_m;
   if ((s = ensure_device(e)) != OMC_OK) return s;
   if ((s = upload_geometry(e->f64, ph, med, rhof, ecut_m.data(), pcut_m.data(), nmed)) != OMC_OK) return s;
   if ((s = upload_geometry(e->f32, ph, med, rhof, ecut_m.data(), pcut_m.data(), nmed)) != OMC_OK) return s;
@@ -1297,7 +1328,7 @@ omc_status run_dij(omc_engine *e, const omc_run_config *cfg, const omc_dij_confi
     cudaMemsetAsync(e->dij_max.p, 0, ng * sizeof(unsigned long long), e->stream);
     cudaMemsetAsync(e->counters.p, 0, sizeof(Counters), e->stream);
     SlotJob job{ng, static_cast<const long long *>(e->dij_first.p), static_cast<const int *>(e->dij_beamlet.p),
-                static_cast<double *>(e->dij_tally.p), first[ng]};
+                static_cast<double *>(e->dij_tally.p), first[ng], nullptr};
     omc_run_stats gs{};
     if (rp.wavefront) s = rp.fp64 ? run_wavefront(e, e->f64, cfg, rp.nlanes, &gs, &job)
                                   : run_wavefront(e, e->f32, cfg, rp.nlanes, &gs, &job);
@@ -1379,6 +1410,200 @@ extern "C" omc_status omc_engine_run_dij(omc_engine *e, const omc_run_config *cf
   }
   *out = d;
   return s;
+}
+
+// ---------------------------------------------------------------------------
+// Resident dose jobs sharing the engine's tables; several jobs advance in
+// one multi-job wavefront launch (a round).
+// ---------------------------------------------------------------------------
+struct omc_job {
+  int precision;
+  long long nperbatch = 0, nhist = 0, done = 0;
+  int nbatch = 0;
+  long long nreg = 0;
+  PrecisionState<float> s32;   // geometry + source when precision is FP32
+  PrecisionState<double> s64;  // ... FP64
+  DevBuf tally;                // [nbatch][nreg]
+  DevBuf ensrc;                // [1]
+  DevBuf result;               // [2][nreg] batch sum and sum of squares
+};
+
+namespace {
+
+// accum = sum over batches, accum2 = sum of squares (accumEndep over the
+// job's batches).
+__global__ void job_accumulate_kernel(const double *tally, int nbatch, long long nreg, double *acc, double *acc2) {
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < nreg;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    double a = 0.0, a2 = 0.0;
+    for (int b = 0; b < nbatch; b++) {
+      double v = tally[static_cast<size_t>(b) * nreg + i];
+      a += v;
+      a2 += v * v;
+    }
+    acc[i] = a;
+    acc2[i] = a2;
+  }
+}
+
+const PrecisionState<float> &job_state(const omc_job *j, float) { return j->s32; }
+const PrecisionState<double> &job_state(const omc_job *j, double) { return j->s64; }
+
+template <typename R>
+JobSlot<R> job_slot(const PrecisionState<R> &S, omc_job *j) {
+  JobSlot<R> js{};
+  js.G = S.G;
+  js.S = S.S;
+  js.tally = static_cast<double *>(j->tally.p);
+  js.ensrc = static_cast<double *>(j->ensrc.p);
+  js.nreg = j->nreg;
+  js.h0 = j->done;
+  js.nperbatch = j->nperbatch;
+  return js;
+}
+
+template <typename R>
+omc_status job_round(omc_engine *e, PrecisionState<R> &S, omc_job *const *jobs, const long long *quota, int n,
+                     const omc_run_config *cfg, omc_run_stats *stats) {
+  const int nlanes = wavefront_blocks<R, true>(e) * kBlock;
+  omc_status s;
+  size_t rng_bytes = static_cast<size_t>(RNG_WORDS) * nlanes * sizeof(int);
+  if (e->rng_u.n < rng_bytes) e->seeded_lanes = 0;
+  if ((s = e->rng_u.ensure(rng_bytes)) != OMC_OK) return s;
+  if ((s = e->rng_ijc.ensure(static_cast<size_t>(3) * nlanes * sizeof(int))) != OMC_OK) return s;
+  if (!(cfg->continue_streams && e->seeded_lanes == nlanes)) {
+    seed_kernel<<<(nlanes + 255) / 256, 256, 0, e->stream>>>(cfg->ixx, cfg->jxx, nlanes,
+                                                            static_cast<int *>(e->rng_u.p),
+                                                            static_cast<int *>(e->rng_ijc.p));
+    e->seeded_lanes = nlanes;
+  }
+  std::vector<JobSlot<R>> slots(n);
+  std::vector<long long> first(n + 1, 0);
+  for (int i = 0; i < n; i++) {
+    slots[i] = job_slot(job_state(jobs[i], R()), jobs[i]);
+    first[i + 1] = first[i] + quota[i];
+  }
+  if ((s = e->multi_slots.ensure(n * sizeof(JobSlot<R>))) != OMC_OK) return s;
+  if ((s = e->multi_first.ensure((n + 1) * sizeof(long long))) != OMC_OK) return s;
+  CUDA_TRY(cudaMemcpyAsync(e->multi_slots.p, slots.data(), n * sizeof(JobSlot<R>), cudaMemcpyHostToDevice,
+                           e->stream));
+  CUDA_TRY(cudaMemcpyAsync(e->multi_first.p, first.data(), (n + 1) * sizeof(long long), cudaMemcpyHostToDevice,
+                           e->stream));
+  CUDA_TRY(cudaMemsetAsync(e->counters.p, 0, sizeof(Counters), e->stream));
+  SlotJob job{n, static_cast<const long long *>(e->multi_first.p), nullptr, nullptr, first[n], e->multi_slots.p};
+  s = run_wavefront(e, S, cfg, nlanes, stats, &job);
+  if (s == OMC_OK || s == OMC_ERR_STACK || s == OMC_ERR_LIMIT)
+    for (int i = 0; i < n; i++) jobs[i]->done += quota[i];
+  return s;
+}
+
+}  // namespace
+
+extern "C" size_t omc_job_device_bytes(const omc_phantom *ph, int nbatch, int precision) {
+  if (!ph) return 0;
+  size_t nreg = static_cast<size_t>(ph->nx) * ph->ny * ph->nz + 1;
+  size_t rsize = precision == OMC_FP32 ? 4 : 8;
+  return nreg * (1 + rsize) + nreg * 8 * (static_cast<size_t>(nbatch > 0 ? nbatch : 1) + 2) +
+         (static_cast<size_t>(ph->nx + ph->ny + ph->nz + 3) + 2 * OMC_INVDIM) * rsize + 4096;
+}
+
+extern "C" omc_status omc_engine_job_add(omc_engine *e, const omc_phantom *ph, const omc_regions *r,
+                                         const omc_source *src, long long nperbatch, int nbatch, int precision,
+                                         omc_job **out) {
+  if (!e || !ph || !r || !src || !out) return fail(OMC_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (!e->f64.tables_ok) return fail(OMC_ERR_STATE, "omc_engine_set_tables must come first");
+  if (nbatch < 1 || nbatch > kBatchTag || nperbatch < 1)
+    return fail(OMC_ERR_ARG, "need 1 <= nbatch <= %d and nperbatch >= 1", kBatchTag);
+  if (precision != OMC_FP32 && precision != OMC_FP64) return fail(OMC_ERR_ARG, "unknown precision");
+  int nmed = e->host_tables_dims.nmed;
+  RegionData rd;
+  omc_status s;
+  if ((s = region_data(nmed, ph, r, rd)) != OMC_OK) return s;
+  if ((s = ensure_device(e)) != OMC_OK) return s;
+  std::unique_ptr<omc_job> j(new omc_job());
+  j->precision = precision;
+  j->nperbatch = nperbatch;
+  j->nbatch = nbatch;
+  j->nhist = nperbatch * nbatch;
+  j->nreg = r->nreg;
+  if (precision == OMC_FP32) {
+    if ((s = upload_geometry(j->s32, ph, rd.med, rd.rhof, rd.ecut_m.data(), rd.pcut_m.data(), nmed)) != OMC_OK)
+      return s;
+    if ((s = upload_source(j->s32, src)) != OMC_OK) return s;
+  } else {
+    if ((s = upload_geometry(j->s64, ph, rd.med, rd.rhof, rd.ecut_m.data(), rd.pcut_m.data(), nmed)) != OMC_OK)
+      return s;
+    if ((s = upload_source(j->s64, src)) != OMC_OK) return s;
+  }
+  if ((s = j->tally.ensure(static_cast<size_t>(nbatch) * j->nreg * sizeof(double))) != OMC_OK) return s;
+  if ((s = j->ensrc.ensure(sizeof(double))) != OMC_OK) return s;
+  if ((s = j->result.ensure(2 * static_cast<size_t>(j->nreg) * sizeof(double))) != OMC_OK) return s;
+  CUDA_TRY(cudaMemset(j->tally.p, 0, static_cast<size_t>(nbatch) * j->nreg * sizeof(double)));
+  CUDA_TRY(cudaMemset(j->ensrc.p, 0, sizeof(double)));
+  *out = j.release();
+  return OMC_OK;
+}
+
+extern "C" long long omc_job_done(const omc_job *j) { return j ? j->done : 0; }
+extern "C" long long omc_job_histories(const omc_job *j) { return j ? j->nhist : 0; }
+
+extern "C" omc_status omc_engine_job_round(omc_engine *e, omc_job *const *jobs, const long long *quota, int njobs,
+                                           const omc_run_config *cfg, omc_run_stats *stats) {
+  if (!e || !jobs || !quota || !cfg || njobs < 1) return fail(OMC_ERR_ARG, "bad argument");
+  if (!e->f64.tables_ok) return fail(OMC_ERR_STATE, "omc_engine_set_tables must come first");
+  if (njobs > (1 << 19)) return fail(OMC_ERR_ARG, "too many jobs in one round");
+  const int prec = jobs[0]->precision;
+  for (int i = 0; i < njobs; i++) {
+    if (!jobs[i] || jobs[i]->precision != prec) return fail(OMC_ERR_ARG, "jobs of one round share one precision");
+    if (quota[i] < 0 || jobs[i]->done + quota[i] > jobs[i]->nhist)
+      return fail(OMC_ERR_ARG, "job %d: quota %lld beyond its remaining histories", i, quota[i]);
+  }
+  omc_status s;
+  if ((s = ensure_device(e)) != OMC_OK) return s;
+  omc_run_stats gs{};
+  s = prec == OMC_FP32 ? job_round(e, e->f32, jobs, quota, njobs, cfg, &gs)
+                       : job_round(e, e->f64, jobs, quota, njobs, cfg, &gs);
+  if (stats) *stats = gs;
+  return s;
+}
+
+extern "C" omc_status omc_engine_job_result(omc_engine *e, omc_job *j, double *accum_endep, double *accum_endep2,
+                                            double *ensrc) {
+  if (!e || !j) return fail(OMC_ERR_ARG, "null argument");
+  omc_status s;
+  if ((s = ensure_device(e)) != OMC_OK) return s;
+  double *acc = static_cast<double *>(j->result.p), *acc2 = acc + j->nreg;
+  job_accumulate_kernel<<<std::max(1, static_cast<int>(std::min<long long>(4 * e->nsm, (j->nreg + 255) / 256))), 256, 0,
+                          e->stream>>>(static_cast<const double *>(j->tally.p), j->nbatch, j->nreg, acc, acc2);
+  if (accum_endep)
+    CUDA_TRY(cudaMemcpyAsync(accum_endep, acc, j->nreg * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+  if (accum_endep2)
+    CUDA_TRY(cudaMemcpyAsync(accum_endep2, acc2, j->nreg * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+  if (ensrc) CUDA_TRY(cudaMemcpyAsync(ensrc, j->ensrc.p, sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+  CUDA_TRY(cudaStreamSynchronize(e->stream));
+  CUDA_TRY(cudaGetLastError());
+  return OMC_OK;
+}
+
+extern "C" void omc_engine_job_remove(omc_engine *e, omc_job *j) {
+  if (!j) return;
+  if (e) cudaSetDevice(e->device);
+  j->s32.geom.clear();
+  j->s32.source.clear();
+  j->s64.geom.clear();
+  j->s64.source.clear();
+  j->tally.release();
+  j->ensrc.release();
+  j->result.release();
+  delete j;
+}
+
+extern "C" omc_status omc_device_memory(int device, size_t *free_bytes, size_t *total_bytes) {
+  if (!free_bytes || !total_bytes) return fail(OMC_ERR_ARG, "null argument");
+  CUDA_TRY(cudaSetDevice(device));
+  CUDA_TRY(cudaMemGetInfo(free_bytes, total_bytes));
+  return OMC_OK;
 }
 
 extern "C" void omc_stream_seeds(int ixx, int jxx, long long k, int *ixx_k, int *jxx_k) {

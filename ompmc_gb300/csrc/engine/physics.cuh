@@ -63,12 +63,15 @@ __device__ __forceinline__ unsigned lanemask_lt() {
   return m;
 }
 
-template <typename R, bool WF>
+template <typename R, bool WF, bool MULTI = false>
 struct Lane {
   const Params<R> &P;
   Ranmar rng;
   int lane;
-  int slot;  // tally slot of the current history / particle (beamlet jobs)
+  int slot;  // tally slot of the current history / particle (beamlet jobs;
+             // multi-job launches: the job slot)
+  int batch; // multi-job launches: batch of the job the particle scores in
+  const JobSlot<R> *js;  // multi-job launches: P.jobs + slot
   int np;    // top slot, -1 = empty (per-lane schedule)
   Particle<R> p;
   bool alive;           // wavefront: p still needs to be queued
@@ -88,6 +91,8 @@ struct Lane {
     rng.stride = sstride;
     np = -1;
     slot = 0;
+    batch = 0;
+    js = nullptr;
     ensrc = 0.0;
     err = 0;
     max_np = 0;
@@ -99,6 +104,30 @@ struct Lane {
   }
 
   __device__ __forceinline__ R rnd() { return static_cast<R>(rng.next_int()) * RC(1.0 / 16777216.0); }
+
+  // Geometry and source of the current particle: the launch's, or its
+  // job's in a multi-job launch.
+  __device__ __forceinline__ const Geometry<R> &geo() const {
+    if constexpr (MULTI) return js->G;
+    else return P.G;
+  }
+  __device__ __forceinline__ const Source<R> &src() const {
+    if constexpr (MULTI) return js->S;
+    else return P.S;
+  }
+  __device__ __forceinline__ int tag_value() const {
+    if constexpr (MULTI) return slot * kBatchTag + batch;
+    else return slot;
+  }
+  __device__ __forceinline__ void set_tag(int t) {
+    if constexpr (MULTI) {
+      slot = t / kBatchTag;
+      batch = t - slot * kBatchTag;
+      js = P.jobs + slot;
+    } else {
+      slot = t;
+    }
+  }
 
   // ---- stack --------------------------------------------------------------
   __device__ __forceinline__ size_t sidx(int slot) const {
@@ -186,14 +215,14 @@ struct Lane {
     __stcg(f + 6 * c + slot, q.w);
     __stcg(f + 7 * c + slot, q.wt);
     __stcg(k + slot, q.ir * 4 + (q.iq + 1));
-    if (tag) __stcg(tag + slot, this->slot);
+    if (tag) __stcg(tag + slot, tag_value());
   }
   __device__ __forceinline__ void emit(const Particle<R> &q) {
     if (q.iq == 0) emit_to(out.ph_f, out.ph_k, out.ph_n, q, out.ph_s);
     else emit_to(out.el_f, out.el_k, out.el_n, q, out.el_s);
   }
   __device__ __forceinline__ void take(const R *f, const int *k, unsigned slot, const int *tag) {
-    if (tag) this->slot = __ldcg(tag + slot);
+    if (tag) set_tag(__ldcg(tag + slot));
     size_t c = queue_cap;
     p.e = __ldcg(f + slot);
     p.x = __ldcg(f + c + slot);
@@ -212,17 +241,20 @@ struct Lane {
   // ---- scoring: ausgab (omc_dosxyz.c:683-694) ------------------------------
   __device__ __forceinline__ void ausgab(int ir, R wt, R edep) {
     n_dep++;
-    atomicAdd(P.endep + static_cast<size_t>(slot) * P.tally_stride + ir, static_cast<double>(wt * edep));
+    if constexpr (MULTI)
+      atomicAdd(js->tally + static_cast<size_t>(batch) * js->nreg + ir, static_cast<double>(wt * edep));
+    else
+      atomicAdd(P.endep + static_cast<size_t>(slot) * P.tally_stride + ir, static_cast<double>(wt * edep));
   }
 
   // ---- geometry: region decode, howfar, hownear (omc_dosxyz.c:187-334) ----
-  __device__ __forceinline__ int med_of(int ir) const { return P.G.med[ir]; }
-  __device__ __forceinline__ R rhof_of(int ir) const { return __ldg(P.G.rhof + ir); }
-  __device__ __forceinline__ R ecut_of(int ir) const { return __ldg(P.G.ecut_m + P.G.med[ir] + 1); }
-  __device__ __forceinline__ R pcut_of(int ir) const { return __ldg(P.G.pcut_m + P.G.med[ir] + 1); }
+  __device__ __forceinline__ int med_of(int ir) const { return geo().med[ir]; }
+  __device__ __forceinline__ R rhof_of(int ir) const { return __ldg(geo().rhof + ir); }
+  __device__ __forceinline__ R ecut_of(int ir) const { return __ldg(geo().ecut_m + geo().med[ir] + 1); }
+  __device__ __forceinline__ R pcut_of(int ir) const { return __ldg(geo().pcut_m + geo().med[ir] + 1); }
 
   __device__ void howfar(const Particle<R> &q, int &idisc, int &irnew, R &ustep) {
-    const Geometry<R> &g = P.G;
+    const Geometry<R> &g = geo();
     n_geom++;
     int irl = q.ir;
     if (irl == 0) {
@@ -275,7 +307,7 @@ struct Lane {
   }
 
   __device__ R hownear(const Particle<R> &q) const {
-    const Geometry<R> &g = P.G;
+    const Geometry<R> &g = geo();
     int irl = q.ir;
     if (irl == 0) return RC(0);
     int irx = (irl - 1) % g.nx;
@@ -388,7 +420,7 @@ struct Lane {
   // Energy and charge of a new history (initHistory's first part, the same
   // in omc_dosxyz.c:970-996 and omc_matrad.c:1092-1123).
   __device__ __forceinline__ void source_energy(Particle<R> &q) {
-    const Source<R> &s = P.S;
+    const Source<R> &s = src();
     q.iq = s.charge;
     R ein;
     if (s.spectrum) {
@@ -400,7 +432,8 @@ struct Lane {
       ein = s.energy;
     }
     q.e = (q.iq != 0) ? ein + RC(0.5109989461) : ein;
-    ensrc += static_cast<double>(ein);
+    if constexpr (MULTI) atomicAdd(js->ensrc, static_cast<double>(ein));
+    else ensrc += static_cast<double>(ein);
   }
 
   // History h of the launch: its tally slot (beamlet jobs), then the
@@ -415,8 +448,15 @@ struct Lane {
       }
       slot = lo;
     }
-    if (P.S.beamlets) init_beamlet_history(__ldg(P.slot_beamlet + slot));
-    else init_point_history();
+    if constexpr (MULTI) {
+      js = P.jobs + slot;
+      const long long hj = js->h0 + (h - __ldg(P.slot_first + slot));
+      batch = static_cast<int>(hj / js->nperbatch);
+      init_point_history();
+    } else {
+      if (P.S.beamlets) init_beamlet_history(__ldg(P.slot_beamlet + slot));
+      else init_point_history();
+    }
   }
 
   // initHistory(ibeamlet) (omc_matrad.c:1084-1254): a uniform point of the
@@ -427,8 +467,8 @@ struct Lane {
   // arithmetic here is rounded operation by operation like the
   // reference's (no fused multiply-adds).
   __device__ void init_beamlet_history(int ib) {
-    const Source<R> &s = P.S;
-    const Geometry<R> &g = P.G;
+    const Source<R> &s = src();
+    const Geometry<R> &g = geo();
     Particle<R> q;
     source_energy(q);
     R rnno1 = rnd();
@@ -495,8 +535,8 @@ struct Lane {
 
   // initHistory (omc_dosxyz.c:964-1068): collimated point source.
   __device__ void init_point_history() {
-    const Source<R> &s = P.S;
-    const Geometry<R> &g = P.G;
+    const Source<R> &s = src();
+    const Geometry<R> &g = geo();
     Particle<R> q;
     source_energy(q);
     R rxyz;

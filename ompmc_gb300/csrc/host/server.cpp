@@ -1,0 +1,365 @@
+// Dose server: continuous batching of dose jobs on one GPU (omc_server_*).
+//
+// Two threads share one engine (tables resident once):
+//  - admission: takes queued jobs in arrival order, maps their media onto
+//    the server's media, builds their regions (initRegions semantics) and
+//    uploads them (omc_engine_job_add) while rounds run on the engine's
+//    compute stream, as far as the device-memory budget and the job limit
+//    allow;
+//  - scheduler: runs rounds over the resident jobs (omc_engine_job_round,
+//    one launch), reads back and frees the jobs that finished, and wakes
+//    their waiters and the admission thread.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "common.h"
+
+using omc::fail;
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct PhantomCopy {
+  int nx = 0, ny = 0, nz = 0;
+  std::vector<double> xb, yb, zb, density;
+  std::vector<int> med;  // indices into the server's media (1-based, 0 vacuum)
+};
+
+enum class JobState { Queued, Resident, Done, Failed };
+
+struct Job {
+  long long id = 0;
+  PhantomCopy ph;
+  omc_source src{};
+  double ecut = 0, pcut = 0;
+  long long nperbatch = 0;
+  int nbatch = 0;
+  size_t bytes = 0;
+  JobState state = JobState::Queued;
+  omc_job *dev = nullptr;
+  std::vector<double> acc, acc2;
+  double ensrc = 0;
+  double submit_s = 0, admit_s = 0, finish_s = 0;
+  int rounds = 0;
+  omc_status status = OMC_OK;
+};
+
+}  // namespace
+
+struct omc_server {
+  omc_server_config cfg{};
+  omc_engine *eng = nullptr;
+  omc_tables *tab = nullptr;
+  std::vector<std::string> media;
+  Clock::time_point t0;
+  std::mutex mu;
+  std::condition_variable cv_admit, cv_sched, cv_done;
+  std::deque<std::shared_ptr<Job>> queued;
+  std::vector<std::shared_ptr<Job>> resident;
+  std::map<long long, std::shared_ptr<Job>> jobs;
+  long long next_id = 1;
+  long long resident_bytes = 0;
+  bool stop = false;
+  omc_server_stats st{};
+  std::thread admit_thread, sched_thread;
+
+  double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
+};
+
+namespace {
+
+// Regions of a job against the server's tables: the phantom with its media
+// renumbered onto the server's, then initRegions (omc_regions_build).
+omc_status upload_job(omc_server *s, Job &j) {
+  omc_status st;
+  std::vector<const char *> names;
+  for (const auto &m : s->media) names.push_back(m.c_str());
+  omc_phantom *ph = nullptr;
+  if ((st = omc_phantom_create(static_cast<int>(names.size()), names.data(), j.ph.nx, j.ph.ny, j.ph.nz,
+                               j.ph.xb.data(), j.ph.yb.data(), j.ph.zb.data(), j.ph.med.data(), j.ph.density.data(),
+                               &ph)) != OMC_OK)
+    return st;
+  char text[256];
+  std::snprintf(text, sizeof text, "global ecut = %.17g\nglobal pcut = %.17g\n", j.ecut, j.pcut);
+  omc_input *in = nullptr;
+  omc_regions *reg = nullptr;
+  if ((st = omc_input_from_string(text, &in)) == OMC_OK && (st = omc_regions_build(in, ph, s->tab, &reg)) == OMC_OK)
+    st = omc_engine_job_add(s->eng, ph, reg, &j.src, j.nperbatch, j.nbatch, s->cfg.precision, &j.dev);
+  omc_regions_free(reg);
+  omc_input_free(in);
+  omc_phantom_free(ph);
+  return st;
+}
+
+void admission_loop(omc_server *s) {
+  std::unique_lock<std::mutex> lk(s->mu);
+  for (;;) {
+    s->cv_admit.wait(lk, [&] {
+      if (s->stop) return true;
+      if (s->queued.empty()) return false;
+      const auto &h = s->queued.front();
+      bool fits = s->resident_bytes + static_cast<long long>(h->bytes) <= s->cfg.hbm_budget ||
+                  s->resident.empty();  // a job larger than the budget still runs, alone
+      return fits && static_cast<int>(s->resident.size()) < s->cfg.max_jobs;
+    });
+    if (s->stop) return;
+    std::shared_ptr<Job> j = s->queued.front();
+    s->queued.pop_front();
+    s->resident_bytes += static_cast<long long>(j->bytes);
+    lk.unlock();
+    omc_status st = upload_job(s, *j);
+    lk.lock();
+    if (st != OMC_OK) {
+      s->resident_bytes -= static_cast<long long>(j->bytes);
+      j->status = st;
+      j->state = JobState::Failed;
+      j->finish_s = s->now();
+      s->cv_done.notify_all();
+      continue;
+    }
+    j->admit_s = s->now();
+    j->state = JobState::Resident;
+    s->resident.push_back(j);
+    s->st.max_resident = std::max(s->st.max_resident, static_cast<int>(s->resident.size()));
+    s->st.max_resident_bytes = std::max(s->st.max_resident_bytes, s->resident_bytes);
+    s->cv_sched.notify_all();
+  }
+}
+
+void scheduler_loop(omc_server *s) {
+  bool seeded = false;
+  std::unique_lock<std::mutex> lk(s->mu);
+  for (;;) {
+    s->cv_sched.wait(lk, [&] { return s->stop || !s->resident.empty(); });
+    if (s->stop) return;
+    std::vector<std::shared_ptr<Job>> round = s->resident;
+    lk.unlock();
+    // Equal shares of the round; a job with fewer histories left takes
+    // only those, and its unused share goes to the others.
+    const long long R = s->cfg.round_histories;
+    std::vector<long long> left(round.size()), quota(round.size(), 0);
+    for (size_t i = 0; i < round.size(); i++) left[i] = omc_job_histories(round[i]->dev) - omc_job_done(round[i]->dev);
+    long long budget = R;
+    size_t open = round.size();
+    while (budget > 0 && open > 0) {
+      long long share = std::max<long long>(1, budget / static_cast<long long>(open));
+      open = 0;
+      for (size_t i = 0; i < round.size(); i++) {
+        long long take = std::min(share, left[i] - quota[i]);
+        if (take <= 0) continue;
+        if (take > budget) take = budget;
+        quota[i] += take;
+        budget -= take;
+        if (left[i] - quota[i] > 0) open++;
+      }
+    }
+    std::vector<omc_job *> devs;
+    std::vector<long long> q;
+    std::vector<std::shared_ptr<Job>> in_round;
+    for (size_t i = 0; i < round.size(); i++)
+      if (quota[i] > 0) {
+        devs.push_back(round[i]->dev);
+        q.push_back(quota[i]);
+        in_round.push_back(round[i]);
+      }
+    omc_status st = OMC_OK;
+    omc_run_stats rs{};
+    if (!devs.empty()) {
+      omc_run_config rc;
+      std::memset(&rc, 0, sizeof rc);
+      rc.nbatch = 1;
+      rc.ixx = s->cfg.ixx;
+      rc.jxx = s->cfg.jxx;
+      rc.nsplit = s->cfg.nsplit;
+      rc.precision = s->cfg.precision;
+      rc.continue_streams = seeded ? 1 : 0;
+      st = omc_engine_job_round(s->eng, devs.data(), q.data(), static_cast<int>(devs.size()), &rc, &rs);
+      seeded = true;
+    }
+    // Jobs that are complete (or hit by a failed round) leave the device.
+    std::vector<std::shared_ptr<Job>> finished;
+    for (auto &j : in_round) {
+      j->rounds++;
+      bool failed_round = st != OMC_OK;
+      if (failed_round || omc_job_done(j->dev) >= omc_job_histories(j->dev)) {
+        if (!failed_round) {
+          j->acc.assign(j->ph.nx * static_cast<size_t>(j->ph.ny) * j->ph.nz + 1, 0.0);
+          j->acc2.assign(j->acc.size(), 0.0);
+          j->status = omc_engine_job_result(s->eng, j->dev, j->acc.data(), j->acc2.data(), &j->ensrc);
+        } else {
+          j->status = st;
+        }
+        omc_engine_job_remove(s->eng, j->dev);
+        j->dev = nullptr;
+        finished.push_back(j);
+      }
+    }
+    lk.lock();
+    s->st.rounds++;
+    s->st.histories += rs.histories;
+    s->st.transport_s += rs.transport_ms * 1e-3;
+    s->st.max_round_jobs = std::max(s->st.max_round_jobs, static_cast<int>(devs.size()));
+    for (auto &j : finished) {
+      j->finish_s = s->now();
+      j->state = j->status == OMC_OK ? JobState::Done : JobState::Failed;
+      s->resident.erase(std::remove(s->resident.begin(), s->resident.end(), j), s->resident.end());
+      s->resident_bytes -= static_cast<long long>(j->bytes);
+      s->st.finished++;
+    }
+    if (!finished.empty()) {
+      s->cv_done.notify_all();
+      s->cv_admit.notify_all();
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" omc_status omc_server_create(const omc_server_config *cfg, const omc_input *data_keys, int nmed,
+                                        const char *const *media, omc_server **out) {
+  if (!cfg || !data_keys || !media || !out) return fail(OMC_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (nmed < 1 || nmed > OMC_MXMED) return fail(OMC_ERR_ARG, "between 1 and %d media", OMC_MXMED);
+  if (cfg->precision != OMC_FP32 && cfg->precision != OMC_FP64) return fail(OMC_ERR_ARG, "unknown precision");
+  std::unique_ptr<omc_server> s(new omc_server());
+  s->cfg = *cfg;
+  if (s->cfg.max_jobs <= 0) s->cfg.max_jobs = 256;
+  if (s->cfg.round_histories <= 0) s->cfg.round_histories = 4000000;
+  if (s->cfg.nsplit <= 0) s->cfg.nsplit = 1;
+  char names[OMC_MXMED][OMC_NAME_LEN];
+  std::memset(names, 0, sizeof names);
+  for (int i = 0; i < nmed; i++) {
+    if (!media[i] || std::strlen(media[i]) >= OMC_NAME_LEN) return fail(OMC_ERR_ARG, "medium name %d", i);
+    std::strcpy(names[i], media[i]);
+    s->media.emplace_back(media[i]);
+  }
+  omc_status st;
+  if ((st = omc_tables_build(data_keys, nmed, names, &s->tab)) != OMC_OK) return st;
+  if ((st = omc_engine_create(cfg->device, &s->eng)) != OMC_OK) {
+    omc_tables_free(s->tab);
+    return st;
+  }
+  if ((st = omc_engine_set_tables(s->eng, s->tab)) != OMC_OK) {
+    omc_engine_destroy(s->eng);
+    omc_tables_free(s->tab);
+    return st;
+  }
+  if (s->cfg.hbm_budget <= 0) {
+    size_t fr = 0, tot = 0;
+    omc_device_memory(cfg->device, &fr, &tot);
+    s->cfg.hbm_budget = static_cast<long long>(fr / 2);
+  }
+  s->t0 = Clock::now();
+  omc_server *raw = s.get();
+  s->admit_thread = std::thread(admission_loop, raw);
+  s->sched_thread = std::thread(scheduler_loop, raw);
+  *out = s.release();
+  return OMC_OK;
+}
+
+extern "C" omc_status omc_server_submit(omc_server *s, const omc_server_job *job, long long *id) {
+  if (!s || !job || !job->phantom || !job->source || !id) return fail(OMC_ERR_ARG, "null argument");
+  if (job->nbatch < 1 || job->nperbatch < 1) return fail(OMC_ERR_ARG, "need nbatch >= 1 and nperbatch >= 1");
+  const omc_phantom *p = job->phantom;
+  auto j = std::make_shared<Job>();
+  j->ph.nx = p->nx;
+  j->ph.ny = p->ny;
+  j->ph.nz = p->nz;
+  size_t nv = static_cast<size_t>(p->nx) * p->ny * p->nz;
+  j->ph.xb.assign(p->xbounds, p->xbounds + p->nx + 1);
+  j->ph.yb.assign(p->ybounds, p->ybounds + p->ny + 1);
+  j->ph.zb.assign(p->zbounds, p->zbounds + p->nz + 1);
+  j->ph.density.assign(p->density, p->density + nv);
+  // Media onto the server's list by name.
+  std::vector<int> map(p->nmed + 1, 0);
+  for (int m = 0; m < p->nmed; m++) {
+    auto it = std::find(s->media.begin(), s->media.end(), std::string(p->med_names[m]));
+    if (it == s->media.end()) return fail(OMC_ERR_MEDIA, "medium %s is not one of the server's", p->med_names[m]);
+    map[m + 1] = static_cast<int>(it - s->media.begin()) + 1;
+  }
+  j->ph.med.resize(nv);
+  for (size_t v = 0; v < nv; v++) {
+    int m = p->med_index[v];
+    if (m < 0 || m > p->nmed) return fail(OMC_ERR_ARG, "voxel %zu: medium %d outside 0..%d", v, m, p->nmed);
+    j->ph.med[v] = map[m];
+  }
+  j->src = *job->source;
+  j->ecut = job->ecut;
+  j->pcut = job->pcut;
+  j->nperbatch = job->nperbatch;
+  j->nbatch = job->nbatch;
+  j->bytes = omc_job_device_bytes(p, job->nbatch, s->cfg.precision);
+  std::lock_guard<std::mutex> lk(s->mu);
+  j->id = s->next_id++;
+  j->submit_s = s->now();
+  s->jobs[j->id] = j;
+  s->queued.push_back(j);
+  s->st.submitted++;
+  *id = j->id;
+  s->cv_admit.notify_all();
+  return OMC_OK;
+}
+
+extern "C" omc_status omc_server_wait(omc_server *s, long long id, double timeout_s, double *accum_endep,
+                                      double *accum_endep2, omc_server_result *res) {
+  if (!s) return fail(OMC_ERR_ARG, "null argument");
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto it = s->jobs.find(id);
+  if (it == s->jobs.end()) return fail(OMC_ERR_ARG, "unknown job %lld", id);
+  std::shared_ptr<Job> j = it->second;
+  auto done = [&] { return j->state == JobState::Done || j->state == JobState::Failed; };
+  if (timeout_s < 0) {
+    s->cv_done.wait(lk, done);
+  } else if (!s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), done)) {
+    return fail(OMC_ERR_LIMIT, "job %lld not finished after %.3f s", id, timeout_s);
+  }
+  s->jobs.erase(it);
+  if (res) {
+    res->ensrc = j->ensrc;
+    res->histories = j->nperbatch * j->nbatch;
+    res->submit_s = j->submit_s;
+    res->admit_s = j->admit_s;
+    res->finish_s = j->finish_s;
+    res->rounds = j->rounds;
+    res->status = j->status;
+  }
+  if (j->state == JobState::Failed) return fail(j->status, "job %lld failed", id);
+  if (accum_endep) std::copy(j->acc.begin(), j->acc.end(), accum_endep);
+  if (accum_endep2) std::copy(j->acc2.begin(), j->acc2.end(), accum_endep2);
+  return OMC_OK;
+}
+
+extern "C" omc_status omc_server_get_stats(omc_server *s, omc_server_stats *st) {
+  if (!s || !st) return fail(OMC_ERR_ARG, "null argument");
+  std::lock_guard<std::mutex> lk(s->mu);
+  *st = s->st;
+  return OMC_OK;
+}
+
+extern "C" void omc_server_destroy(omc_server *s) {
+  if (!s) return;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+  }
+  s->cv_admit.notify_all();
+  s->cv_sched.notify_all();
+  if (s->admit_thread.joinable()) s->admit_thread.join();
+  if (s->sched_thread.joinable()) s->sched_thread.join();
+  for (auto &j : s->resident)
+    if (j->dev) omc_engine_job_remove(s->eng, j->dev);
+  s->resident.clear();
+  omc_engine_destroy(s->eng);
+  omc_tables_free(s->tab);
+  delete s;
+}

@@ -59,18 +59,19 @@ def homogeneous(n=60, vox=0.5, medium=WATER, rho=1.0, nxyz=None):
 
 
 def slab(n=150, vox=0.2, layers=((0.0, 5.0, WATER, 1.0), (5.0, 15.0, LUNG, 0.26),
-                                 (15.0, 18.0, BONE, 1.85), (18.0, 30.0, WATER, 1.0))):
+                                 (15.0, 18.0, BONE, 1.85), (18.0, 30.0, WATER, 1.0)), nxyz=None):
     """z-slabs; each layer is (z_lo, z_hi, medium, density) in cm."""
-    xb = _bounds(n, vox, -0.5 * n * vox)
-    yb = _bounds(n, vox, -0.5 * n * vox)
-    zb = _bounds(n, vox, 0.0)
+    nx, ny, nz = nxyz if nxyz else (n, n, n)
+    xb = _bounds(nx, vox, -0.5 * nx * vox)
+    yb = _bounds(ny, vox, -0.5 * ny * vox)
+    zb = _bounds(nz, vox, 0.0)
     media = []
     for _, _, m, _ in layers:
         if m not in media:
             media.append(m)
     zc = 0.5 * (zb[:-1] + zb[1:])
-    med = np.zeros((n, n, n), np.uint8)
-    dens = np.zeros((n, n, n), np.float64)
+    med = np.zeros((nz, ny, nx), np.uint8)
+    dens = np.zeros((nz, ny, nx), np.float64)
     for lo, hi, m, rho in layers:
         sel = (zc >= lo) & (zc < hi)
         med[sel] = media.index(m) + 1

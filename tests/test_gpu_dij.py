@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 from cases import DIJ_CASES, dij_case
 from conftest import GOLDEN
-from stats import consistent
+from stats import compare_runs, consistent
 
 from ompmc_gb300 import _native as N
 from ompmc_gb300 import api
@@ -67,21 +67,16 @@ def test_tally_groups_do_not_change_the_result(engine, dij_problem):
     np.testing.assert_array_equal(c[2], a[2].astype(np.float32))
 
 
-def _repeat(fn, k):
-    runs = np.stack([fn(i) for i in range(k)])
-    return runs.sum(0), (runs * runs).sum(0)
-
-
 @pytest.mark.parametrize("precision", [api.FP64, api.FP32])
 @pytest.mark.parametrize("schedule", [api.WAVEFRONT, api.LANES])
 def test_many_lanes_dij_statistically_identical(precision, schedule, engine, oracle, dij_problem):
-    """K = 10 independent dij runs (different seeds) of the GPU and of the
-    OpenMP oracle, threshold 0: per (beamlet, voxel) z-scores over entries
-    above 20% of the beamlet maximum are consistent with one distribution,
-    and the total dose agrees within 6/sqrt(N)."""
+    """K = 16 independent dij runs (different seeds) of the GPU and of the
+    OpenMP oracle, threshold 0: the per (beamlet, voxel) Welch statistics
+    over entries above 20% of the beamlet maximum are consistent with one
+    distribution, and so are the totals (|t| < 4)."""
     prob, bl, _ = dij_problem("dij_slab", ncase=2000, nbatch=2)
     nrows = prob.nreg - 1
-    k = 10
+    k = 16
 
     def gpu(i):
         col, rows, vals, st = engine.run_dij(rel_threshold=0.0, precision=precision, schedule=schedule,
@@ -93,23 +88,10 @@ def test_many_lanes_dij_statistically_identical(precision, schedule, engine, ora
         col, rows, vals, _ = oracle.run_dij(prob, bl, rel_threshold=0.0, seeds=(211 + i, 7 + 5 * i), nthreads=0)
         return dense(col, rows, vals, nrows)
 
-    g, g2 = _repeat(gpu, k)
-    o, o2 = _repeat(cpu, k)
-    c = _compare_rows(g, g2, o, o2, k)
+    c = compare_runs(np.stack([gpu(i) for i in range(k)]), np.stack([cpu(i) for i in range(k)]))
     assert c["n"] > 200, c
     assert consistent(c), c
-    assert abs(c["etot_rel"]) < 6.0 / np.sqrt(k * 2000 * bl.n), c
-
-
-def _compare_rows(a, a2, b, b2, k):
-    ma, mb = a / k, b / k
-    va = np.maximum(a2 / k - ma * ma, 0) / (k - 1)
-    vb = np.maximum(b2 / k - mb * mb, 0) / (k - 1)
-    sel = mb > 0.2 * mb.max(axis=1, keepdims=True)
-    sig = np.sqrt(va[sel] + vb[sel])
-    z = (ma[sel] - mb[sel]) / np.where(sig > 0, sig, np.inf)
-    return {"n": int(sel.sum()), "frac_2sigma": float(np.mean(np.abs(z) <= 2)), "mean_z2": float(np.mean(z * z)),
-            "etot_rel": float(ma.sum() / mb.sum() - 1)}
+    assert abs(c["t_total"]) < 4.0, c
 
 
 def test_uneven_histories_per_beamlet(engine, oracle, dij_problem):
