@@ -433,8 +433,10 @@ def run_serve_leg(args, local_rank):
         media = [W.AIR, W.LUNG, W.WATER, W.BONE]
         data_text = f"pegs file = {P['pegs']}\npgs4form file = {P['pgs4form']}\ndata folder = {P['data_folder']}\n"
         out = {}
-        for mode, max_jobs in (("continuous", 0), ("one_at_a_time", 1)):
-            srv = api.Server(media, data_text, precision=api.FP32, max_jobs=max_jobs)
+        modes = (("continuous", 0, api.Server.SHORTEST_FIRST), ("continuous_equal_shares", 0, api.Server.EQUAL_SHARES),
+                 ("one_at_a_time", 1, api.Server.SHORTEST_FIRST))
+        for mode, max_jobs, policy in modes:
+            srv = api.Server(media, data_text, precision=api.FP32, max_jobs=max_jobs, policy=policy)
             # warm-up job (tables, kernels)
             srv.wait(srv.submit(phs[0], sources.get((0, 0)) or api.build_source(inputs[0], phs[0]), 0.7, 0.01,
                                 1000, 10))
@@ -460,7 +462,8 @@ def run_serve_leg(args, local_rank):
                 "dtype": "f32", "config": {"workload": SERVE_WORKLOAD, "jobs": njobs, "rate_per_s": args.serve_rate,
                                            "mean_histories": mean_h, "total_histories": total,
                                            "seed": args.serve_seed},
-                "continuous": out["continuous"], "one_at_a_time": out["one_at_a_time"]}
+                "continuous": out["continuous"], "continuous_equal_shares": out["continuous_equal_shares"],
+                "one_at_a_time": out["one_at_a_time"]}
 
 
 def main():

@@ -480,7 +480,13 @@ typedef struct omc_server_config {
                                    jobs; 0 = 4,000,000                     */
     int nsplit;                 /* photon splitting, every job (0 = 1)     */
     int ixx, jxx;               /* RANMAR seeds of the server's streams    */
+    int policy;                 /* round quotas: OMC_SERVE_SHORTEST_FIRST
+                                   (fill the round with the jobs that have
+                                   the fewest histories left; default) or
+                                   OMC_SERVE_EQUAL_SHARES                  */
 } omc_server_config;
+
+enum { OMC_SERVE_SHORTEST_FIRST = 0, OMC_SERVE_EQUAL_SHARES = 1 };
 
 /* The server's media: every job's phantom media must be among them.
  * data_keys supplies "pegs file", "pgs4form file" and "data folder"; the

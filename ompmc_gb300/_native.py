@@ -105,7 +105,8 @@ class MatradOpt_t(C.Structure):
 
 class ServerConfig_t(C.Structure):
     _fields_ = [("device", C.c_int), ("precision", C.c_int), ("hbm_budget", C.c_longlong), ("max_jobs", C.c_int),
-                ("round_histories", C.c_longlong), ("nsplit", C.c_int), ("ixx", C.c_int), ("jxx", C.c_int)]
+                ("round_histories", C.c_longlong), ("nsplit", C.c_int), ("ixx", C.c_int), ("jxx", C.c_int),
+                ("policy", C.c_int)]
 
 
 class ServerJob_t(C.Structure):

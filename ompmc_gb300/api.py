@@ -273,11 +273,13 @@ class Server:
     GPU.  `media` are the server's pegs4 media; `data_text` is .inp text
     with the "pegs file", "pgs4form file" and "data folder" keys."""
 
+    SHORTEST_FIRST, EQUAL_SHARES = 0, 1
+
     def __init__(self, media, data_text, precision=FP32, hbm_budget=0, max_jobs=0, round_histories=0, nsplit=1,
-                 seeds=(97, 33), device=0):
+                 seeds=(97, 33), device=0, policy=0):
         self._inp = Input(text=data_text)
         cfg = N.ServerConfig_t(device, precision, int(hbm_budget), int(max_jobs), int(round_histories),
-                               int(nsplit), int(seeds[0]), int(seeds[1]))
+                               int(nsplit), int(seeds[0]), int(seeds[1]), int(policy))
         names = (C.c_char_p * len(media))(*[m.encode() for m in media])
         self._h = C.c_void_p()
         check(N.lib().omc_server_create(C.byref(cfg), self._inp._h, len(media), names, C.byref(self._h)))

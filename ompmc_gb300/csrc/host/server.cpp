@@ -144,23 +144,37 @@ void scheduler_loop(omc_server *s) {
     if (s->stop) return;
     std::vector<std::shared_ptr<Job>> round = s->resident;
     lk.unlock();
-    // Equal shares of the round; a job with fewer histories left takes
-    // only those, and its unused share goes to the others.
     const long long R = s->cfg.round_histories;
     std::vector<long long> left(round.size()), quota(round.size(), 0);
     for (size_t i = 0; i < round.size(); i++) left[i] = omc_job_histories(round[i]->dev) - omc_job_done(round[i]->dev);
     long long budget = R;
-    size_t open = round.size();
-    while (budget > 0 && open > 0) {
-      long long share = std::max<long long>(1, budget / static_cast<long long>(open));
-      open = 0;
-      for (size_t i = 0; i < round.size(); i++) {
-        long long take = std::min(share, left[i] - quota[i]);
-        if (take <= 0) continue;
-        if (take > budget) take = budget;
-        quota[i] += take;
-        budget -= take;
-        if (left[i] - quota[i] > 0) open++;
+    if (s->cfg.policy == OMC_SERVE_EQUAL_SHARES) {
+      // Equal shares; a job with fewer histories left takes only those and
+      // its unused share goes to the others.
+      size_t open = round.size();
+      while (budget > 0 && open > 0) {
+        long long share = std::max<long long>(1, budget / static_cast<long long>(open));
+        open = 0;
+        for (size_t i = 0; i < round.size(); i++) {
+          long long take = std::min(share, left[i] - quota[i]);
+          if (take <= 0) continue;
+          if (take > budget) take = budget;
+          quota[i] += take;
+          budget -= take;
+          if (left[i] - quota[i] > 0) open++;
+        }
+      }
+    } else {
+      // Shortest remaining first: the round is filled with the jobs that
+      // have the fewest histories left (arrival order among equals), so
+      // small jobs finish in the next round and large ones take the rest.
+      std::vector<size_t> order(round.size());
+      for (size_t i = 0; i < order.size(); i++) order[i] = i;
+      std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return left[a] < left[b]; });
+      for (size_t i : order) {
+        if (budget <= 0) break;
+        quota[i] = std::min(left[i], budget);
+        budget -= quota[i];
       }
     }
     std::vector<omc_job *> devs;

@@ -65,7 +65,7 @@ def test_job_same_alone_and_in_mix(native, problem_factory):
               problem_factory("slab_250kvp", ncase=300000, nbatch=10, seeds=(5, 6)),
               problem_factory("electron_pencil", ncase=40000, nbatch=10, seeds=(7, 8)),
               problem_factory("positron_field", ncase=40000, nbatch=10, seeds=(9, 10))]
-    srv = api.Server(MEDIA, data_text(), precision=api.FP32, round_histories=150000)
+    srv = api.Server(MEDIA, data_text(), precision=api.FP32, round_histories=150000, policy=api.Server.EQUAL_SHARES)
     try:
         alone = srv.wait(srv.submit_problem(a_prob))
         ids = [srv.submit_problem(p) for p in others[:2]]
@@ -108,10 +108,11 @@ def test_admission_respects_budget(native, problem_factory):
         assert r1.admit_s >= r0.finish_s - 1e-3
 
 
-def test_small_job_overtakes_large_one(native, problem_factory):
+@pytest.mark.parametrize("policy", [0, 1])
+def test_small_job_overtakes_large_one(policy, native, problem_factory):
     big = problem_factory("slab_6mv", ncase=4000000, nbatch=10, seeds=(21, 22))
     small = problem_factory("water_mono", ncase=20000, nbatch=10, seeds=(23, 24))
-    srv = api.Server(MEDIA, data_text(), precision=api.FP32, round_histories=400000)
+    srv = api.Server(MEDIA, data_text(), precision=api.FP32, round_histories=400000, policy=policy)
     try:
         b = srv.submit_problem(big)
         s = srv.submit_problem(small)

@@ -177,3 +177,25 @@ def test_stream_seed_rule(native):
     assert api.stream_seeds(31328, 31328, 1) == (1, 1)
     pairs = {api.stream_seeds(97, 33, k) for k in range(0, 200000, 7)}
     assert len(pairs) == len(range(0, 200000, 7))
+
+
+def test_3ddose_text_is_printf_byte_for_byte(native, tmp_path, problem_factory):
+    """The parallel .3ddose writer produces exactly the reference's
+    fprintf("%e ") / fprintf("%f ") text (outputResults,
+    omc_dosxyz.c:842-879), edge values included."""
+    import numpy as np
+
+    prob = problem_factory("slab_6mv")
+    rng = np.random.default_rng(3)
+    n = prob.nreg
+    d = rng.random(n) * 10.0 ** rng.integers(-300, 300, n)
+    u = rng.random(n) * 10.0 ** rng.integers(-9, 17, n)
+    d[1:6] = [0.0, -0.0, 5e-324, 0.5e-6, 9.9999995e-5]
+    u[1:4] = [0.9999999, 0.0000005, 1e17]
+    path = str(tmp_path / "x.3ddose")
+    prob.write_3ddose(path, d, u)
+    lines = open(path).read().split("\n")
+    s = prob.phantom.s
+    assert lines[0] == "%5d%5d%5d" % (s.nx, s.ny, s.nz)
+    assert lines[4] == "".join("%e " % x for x in d[1:])
+    assert lines[5] == "".join("%f " % x for x in u[1:])
