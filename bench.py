@@ -374,6 +374,68 @@ def run_dij_leg(args, local_rank):
         return line
 
 
+CT_WORKLOAD = ("CT-like blob phantom 256x256x128 @ 2 mm (seed 2024), synthetic 6 MV, point source SSD 100 cm; "
+               "fields 3x3 and 10x10 cm2 at gantry 0 (+z) and gantry 90 (phantom axes x and z exchanged so that "
+               "the beam enters along +z)")
+
+
+def run_ct_leg(args, local_rank):
+    """FP32-transport dose error against an FP64 run of the same engine, per
+    field, on the CT-like phantom: both precisions with the same histories
+    in 10 batches; per-voxel z over voxels above 20% of Dmax (t-corrected),
+    mean relative difference over voxels above 50% of Dmax, total energy."""
+    import torch
+    from scipy import stats as S
+
+    from ompmc_gb300 import api, data
+    from ompmc_gb300 import workloads as W
+
+    torch.cuda.set_device(local_rank)
+    data.stage()
+    P = data.paths()
+    H = args.ct_histories
+    nb = 10
+    ph0 = W.ct_like()
+    # gantry 90: exchange x and z (arrays [z, y, x] -> [x, y, z])
+    ph90 = W.Phantom(ph0.media, ph0.zb - ph0.zb.mean(), ph0.yb, ph0.xb - ph0.xb[0],
+                     np.ascontiguousarray(ph0.med.transpose(2, 1, 0)),
+                     np.ascontiguousarray(ph0.rho.transpose(2, 1, 0)))
+    fields = []
+    with tempfile.TemporaryDirectory() as tmp:
+        spec = W.write_spectrum(os.path.join(tmp, "6mv.spectrum"), "synthetic 6 MV", *W.spectrum_6mv())
+        for gname, ph in (("gantry0", ph0), ("gantry90", ph90)):
+            phantom = api.Phantom.from_arrays(ph.media, ph.xb, ph.yb, ph.zb, ph.med, ph.rho)
+            for half in (1.5, 5.0):
+                job = W.Job("(in memory)", P["pegs"], P["pgs4form"], P["data_folder"], tmp + os.sep,
+                            spectrum_file=spec, ncase=H, nbatch=nb, collimator=(-half, half, -half, half), ssd=100.0)
+                prob = api.Problem(api.Input(text=job.text()), phantom=phantom)
+                eng = api.Engine(local_rank).load(prob)
+                eng.run(nperbatch=100000, nbatch=1, precision=api.FP32)  # warm-up
+                a32, b32, s32 = eng.run(precision=api.FP32, seeds=(97, 33))
+                a64, b64, s64 = eng.run(precision=api.FP64, seeds=(12, 34))
+                eng.close()
+                m32, m64 = a32[1:] / nb, a64[1:] / nb
+                v32 = np.maximum(b32[1:] / nb - m32 ** 2, 0) / (nb - 1)
+                v64 = np.maximum(b64[1:] / nb - m64 ** 2, 0) / (nb - 1)
+                sel = m64 > 0.2 * m64.max()
+                tz = (m32[sel] - m64[sel]) / np.sqrt(v32[sel] + v64[sel])
+                z = S.norm.ppf(np.clip(S.t.cdf(tz, 2 * (nb - 1)), 1e-300, 1 - 1e-16))
+                hi = m64 > 0.5 * m64.max()
+                rel = (m32[hi] - m64[hi]) / m64[hi]
+                fields.append({"field": f"{gname} {2 * half:g}x{2 * half:g} cm2", "histories": H,
+                               "fp32_histories_per_s": H / (s32.kernel_ms / 1e3),
+                               "fp64_histories_per_s": H / (s64.kernel_ms / 1e3),
+                               "voxels_above_20pct": int(sel.sum()),
+                               "frac_within_2sigma": float(np.mean(np.abs(z) <= 2)),
+                               "mean_z2": float(np.mean(z * z)),
+                               "mean_rel_diff_above_50pct": float(rel.mean()),
+                               "sigma_of_mean_rel_diff": float(np.sqrt(np.mean((v32[hi] + v64[hi]) / m64[hi] ** 2)
+                                                                       / hi.sum())),
+                               "total_energy_rel_diff": float(a32[1:].sum() / a64[1:].sum() - 1)})
+    return {"metric": "FP32-transport dose error vs FP64, per field", "n_gpus": 1, "data": "synthetic",
+            "config": {"workload": CT_WORKLOAD, "batches": nb}, "fields": fields}
+
+
 SERVE_WORKLOAD = ("dose-server mix: Poisson arrivals; phantom homogeneous water / z-slab / seeded blob at 64^3, "
                   "128^3 or 256x256x160 (2-4.7 mm voxels over a 30-48 cm box); source 1.25 MeV, synthetic 6 MV or "
                   "synthetic 250 kVp, 10x10 cm2 field at SSD 100 cm; histories log-uniform over [1e5, 1e8]; "
@@ -478,6 +540,8 @@ def main():
     ap.add_argument("--dij", action="store_true", help="measure the batched dij workload instead (one JSON line)")
     ap.add_argument("--dij-scale", type=float, default=1.0, help="scale of the dij history counts")
     ap.add_argument("--serve", action="store_true", help="measure the dose-server mix instead (one JSON line)")
+    ap.add_argument("--ct", action="store_true", help="FP32-vs-FP64 dose error per field on the CT-like phantom")
+    ap.add_argument("--ct-histories", type=int, default=20_000_000)
     ap.add_argument("--serve-jobs", type=int, default=40)
     ap.add_argument("--serve-rate", type=float, default=0.5, help="job arrivals per second")
     ap.add_argument("--serve-max-histories", type=float, default=1e8)
@@ -494,6 +558,10 @@ def main():
     if args.dij:
         if rank == 0:
             print(json.dumps(run_dij_leg(args, local_rank)), flush=True)
+        return
+    if args.ct:
+        if rank == 0:
+            print(json.dumps(run_ct_leg(args, local_rank)), flush=True)
         return
     if args.serve:
         if rank == 0:

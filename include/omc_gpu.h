@@ -339,6 +339,14 @@ omc_status omc_engine_run_resident(omc_engine *e, const omc_run_config *cfg,
 omc_status omc_engine_run_noalloc(omc_engine *e, const omc_run_config *cfg,
                                   double *d_endep, omc_run_stats *stats);
 
+/* Diagnostics: record, for each iteration of the next wavefront launches
+ * (at most `iterations`; 0 switches recording off), the device time in ns
+ * and the photons, electrons and histories in flight at its start.
+ * omc_engine_trace_read copies the records of the last launch, 4 values
+ * each, and their number. */
+omc_status omc_engine_trace(omc_engine *e, int iterations);
+omc_status omc_engine_trace_read(omc_engine *e, long long *out, int cap, int *n);
+
 /* Free and total device memory of a CUDA device (bytes). */
 omc_status omc_device_memory(int device, size_t *free_bytes, size_t *total_bytes);
 

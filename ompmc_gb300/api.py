@@ -259,6 +259,19 @@ class Engine:
         col_ptr, rows, vals = _take_dij(out, fp32_values)
         return col_ptr, rows, vals, st
 
+    def trace(self, iterations):
+        """Record per-iteration device time and queue sizes of the next
+        wavefront launches (0 = off)."""
+        check(N.lib().omc_engine_trace(self._h, int(iterations)))
+
+    def trace_read(self, cap=1 << 16):
+        """[n, 4] int64: ns, photons, electrons, histories injected, per
+        iteration of the last wavefront launch."""
+        out = np.zeros((cap, 4), np.int64)
+        n = C.c_int()
+        check(N.lib().omc_engine_trace_read(self._h, out.ctypes.data_as(C.POINTER(C.c_longlong)), cap, C.byref(n)))
+        return out[:n.value]
+
     def close(self):
         if getattr(self, "_h", None):
             N.lib().omc_engine_destroy(self._h)

@@ -161,6 +161,8 @@ struct Wavefront {
   int max_iters;
   int *iters;             // iterations used (output)
   unsigned *hwm;          // queue high-water mark (output)
+  unsigned long long *trace;  // per iteration {ns, photons, electrons, injected}, or null
+  int trace_cap;              // iterations the trace holds
 };
 
 constexpr long long kBarrierSpinCap = 1ll << 28;  // x ~64 ns: well past any phase
@@ -223,6 +225,15 @@ __global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) wavefront_ke
     const unsigned long long injected = *static_cast<volatile unsigned long long *>(W.injected + bin);
     const long long remaining = P.nhist - static_cast<long long>(injected);
     const unsigned long long inflight = static_cast<unsigned long long>(n_ph) + n_el;
+    if (W.trace && gtid == 0 && it < W.trace_cap) {
+      unsigned long long ns;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(ns));
+      unsigned long long *r = W.trace + 4 * static_cast<size_t>(it);
+      r[0] = ns;
+      r[1] = n_ph;
+      r[2] = n_el;
+      r[3] = injected;
+    }
     if (remaining <= 0 && inflight == 0) break;
     long long m = static_cast<long long>(W.target) - static_cast<long long>(inflight);
     if (m < 0) m = 0;
@@ -547,6 +558,10 @@ struct omc_engine {
   DevBuf dij_tally, dij_first, dij_beamlet, dij_nhist, dij_max, dij_cnt, dij_off, dij_rows, dij_vals;
   // multi-job rounds
   DevBuf multi_slots, multi_first;
+  // per-iteration trace of the last wavefront launch (diagnostics)
+  DevBuf trace;
+  int trace_cap = 0;
+  int trace_iters = 0;
   // host copies needed across uploads
   omc_tables host_tables_dims{};
 };
@@ -930,6 +945,8 @@ omc_status run_wavefront(omc_engine *e, PrecisionState<R> &S, const omc_run_conf
   W.max_iters = 1 << 21;
   W.iters = &wc->iters;
   W.hwm = &wc->hwm;
+  W.trace = static_cast<unsigned long long *>(e->trace.p);
+  W.trace_cap = e->trace_cap;
   Counters *dc = static_cast<Counters *>(e->counters.p);
   Params<R> P{};
   P.T = S.T;
@@ -981,6 +998,7 @@ omc_status run_wavefront(omc_engine *e, PrecisionState<R> &S, const omc_run_conf
   cudaMemcpy(&hc, dc, sizeof hc, cudaMemcpyDeviceToHost);
   cudaMemcpy(&hw, wc, sizeof hw, cudaMemcpyDeviceToHost);
   iters_total = hw.iters;
+  e->trace_iters = hw.iters;
   if (stats) {
     stats->ensrc = hc.ensrc;
     stats->transport_ms = ms;
@@ -1066,7 +1084,7 @@ extern "C" void omc_engine_destroy(omc_engine *e) {
   e->f64.beamlets.clear();
   e->f32.beamlets.clear();
   for (DevBuf *b : {&e->dij_tally, &e->dij_first, &e->dij_beamlet, &e->dij_nhist, &e->dij_max, &e->dij_cnt,
-                    &e->dij_off, &e->dij_rows, &e->dij_vals, &e->multi_slots, &e->multi_first})
+                    &e->dij_off, &e->dij_rows, &e->dij_vals, &e->multi_slots, &e->multi_first, &e->trace})
     b->release();
   cudaStreamDestroy(e->stream);
   delete e;
@@ -1597,6 +1615,31 @@ extern "C" void omc_engine_job_remove(omc_engine *e, omc_job *j) {
   j->ensrc.release();
   j->result.release();
   delete j;
+}
+
+extern "C" omc_status omc_engine_trace(omc_engine *e, int iterations) {
+  if (!e || iterations < 0) return fail(OMC_ERR_ARG, "bad argument");
+  omc_status s;
+  if ((s = ensure_device(e)) != OMC_OK) return s;
+  if (iterations == 0) {
+    e->trace.release();
+    e->trace_cap = 0;
+    return OMC_OK;
+  }
+  if ((s = e->trace.ensure(static_cast<size_t>(iterations) * 4 * sizeof(unsigned long long))) != OMC_OK) return s;
+  e->trace_cap = iterations;
+  return OMC_OK;
+}
+
+extern "C" omc_status omc_engine_trace_read(omc_engine *e, long long *out, int cap, int *n) {
+  if (!e || !out || !n) return fail(OMC_ERR_ARG, "null argument");
+  omc_status s;
+  if ((s = ensure_device(e)) != OMC_OK) return s;
+  int k = std::min(std::min(cap, e->trace_cap), e->trace_iters + 1);
+  *n = k < 0 ? 0 : k;
+  if (*n > 0) CUDA_TRY(cudaMemcpy(out, e->trace.p, static_cast<size_t>(*n) * 4 * sizeof(long long),
+                                  cudaMemcpyDeviceToHost));
+  return OMC_OK;
 }
 
 extern "C" omc_status omc_device_memory(int device, size_t *free_bytes, size_t *total_bytes) {
