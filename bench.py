@@ -209,73 +209,62 @@ def run_ours(args, rank, world, local_rank, dist_on):
         eng = api.Engine(local_rank).load(prob)
         seeds = D.rank_seeds(97, 33, rank, LANES_PER_RANK_STRIDE)
         H = args.histories_per_step
+        K = args.steps
         cfg32 = api.Engine.config(H, 1, seeds=seeds, precision=api.FP32)
-        # warm-up
+        # warm-up: single batches of the same size
         for _ in range(args.warmup):
             flush_l2()
-            eng.run_resident(cfg32)  # seeds the streams the timed batches continue
-        # timed region: K batches of H histories, FP32 transport / FP64 tallies
+            eng.run_resident(cfg32)  # seeds the streams the timed job continues
+        # timed region: the K-batch job of K*H histories, FP32 transport /
+        # FP64 tallies.  The engine transports all batches of a job in one
+        # launch (batch tallies side by side, 270 MB > L2), so a step is one
+        # of its batches.
         sampler = ClockSampler(local_rank)
+        flush_l2()
         barrier()
         sampler.start()
-        step_ms, geo, dep, evs = [], 0, 0, 0
-        acc = np.zeros(prob.nreg)
-        acc2 = np.zeros(prob.nreg)
-        launches = 0
-        for k in range(args.steps):
-            flush_l2()
-            # successive batches of one job: the streams continue
-            a, _, st = eng.run(nperbatch=H, nbatch=1, seeds=seeds, precision=api.FP32, continue_streams=1)
-            if st.error_flags:
-                raise RuntimeError(f"device error flags {st.error_flags:#x}")
-            step_ms.append(st.kernel_ms)
-            geo += st.voxel_steps
-            dep += st.deposits
-            evs += st.steps
-            acc += a
-            acc2 += a * a
-            launches += 2  # wavefront transport, batch accumulation (streams continue: no seeding)
+        acc, acc2, st = eng.run(nperbatch=H, nbatch=K, seeds=seeds, precision=api.FP32, continue_streams=1)
         barrier()
         clocks = sampler.stop()
-        dev_ms = float(sum(step_ms))
+        if st.error_flags:
+            raise RuntimeError(f"device error flags {st.error_flags:#x}")
+        dev_ms = float(st.kernel_ms)
+        geo, dep, evs = st.voxel_steps, st.deposits, st.steps
+        launches = 2  # wavefront transport of all batches, batch accumulation (streams continue: no seeding)
         if dist_on:
             import torch.distributed as tdist
 
             t = torch.tensor([dev_ms], dtype=torch.float64, device=f"cuda:{local_rank}")
             tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
             dev_ms = float(t.item())
-        total_hist = world * args.steps * H
+        total_hist = world * K * H
         value = total_hist / (dev_ms / 1000.0)
-        s = max_rel_sigma(acc, acc2, args.steps) if args.steps >= 2 else None
+        s = max_rel_sigma(acc, acc2, K) if K >= 2 else None
         efficiency = 1.0 / (s * s * dev_ms / 1000.0) if s else None
-        # plain FP64 path, same workload, fewer histories
-        cfg64 = api.Engine.config(FP64_HISTORIES, 1, seeds=seeds, precision=api.FP64)
-        eng.run_resident(cfg64)
-        f64 = []
-        for _ in range(2):
-            flush_l2()
-            _, _, st = eng.run_resident(cfg64)
-            f64.append(st.kernel_ms)
-        fp64_value = FP64_HISTORIES / (statistics.mean(f64) / 1000.0)
-        # end to end through the C ABI: phantom upload, transport, tallies back
-        e2e_steps = max(1, min(args.steps, 3))
+        # plain FP64 path, same workload and job structure, fewer histories
+        H64 = FP64_HISTORIES // K
+        eng.run(nperbatch=H64 // 4, nbatch=K, seeds=seeds, precision=api.FP64)
+        flush_l2()
+        _, _, st64 = eng.run(nperbatch=H64, nbatch=K, seeds=seeds, precision=api.FP64)
+        fp64_value = H64 * K / (st64.kernel_ms / 1000.0)
+        # end to end through the C ABI: phantom upload, the K-batch job,
+        # batch sums back in host memory
         ph = prob.phantom
         regs = prob.regions
         h2d = prob.nreg * (1 + 4 + 8) + 8 * (sum(ph.shape) + 3) * 2
         d2h = 2 * prob.nreg * 8
         barrier()
         t0 = time.perf_counter()
-        for k in range(e2e_steps):
-            eng.set_geometry(prob)
-            a, a2, st = eng.run(nperbatch=H, nbatch=1, seeds=seeds, precision=api.FP32)
+        eng.set_geometry(prob)
+        a, a2, st_e2e = eng.run(nperbatch=H, nbatch=K, seeds=seeds, precision=api.FP32)
         torch.cuda.synchronize()
         e2e_s = time.perf_counter() - t0
-        e2e_value = world * e2e_steps * H / e2e_s
+        e2e_value = world * K * H / e2e_s
         # roofline of the transport kernel
         peak, peak_kind = measured_peaks()
-        per_hist_bytes = (8.0 * geo + 8.0 * dep) / (args.steps * H) + 16.0
-        launch_s = dev_ms / 1000.0 / args.steps
-        achieved = per_hist_bytes * H / launch_s / 1e9
+        per_hist_bytes = (8.0 * geo + 8.0 * dep) / (K * H) + 16.0
+        launch_s = dev_ms / 1000.0
+        achieved = per_hist_bytes * K * H / launch_s / 1e9
         traffic_ph = profiled_traffic()
         line = None
         if rank == 0:
@@ -284,7 +273,6 @@ def run_ours(args, rank, world, local_rank, dist_on):
                 rate, cores, n, secs = cpu_oracle_sample(prob)
                 cpu = {"value": rate, "unit": "histories/s", "cores": cores, "kind": "port",
                        "sample": f"{n} histories of the workload (oracle port, OpenMP dynamic schedule), {secs:.1f} s"}
-            lat = sorted(step_ms)
             line = {
                 "metric": "histories/s", "value": value, "unit": "histories/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms / args.steps,
@@ -292,17 +280,21 @@ def run_ours(args, rank, world, local_rank, dist_on):
                 "data": "synthetic",
                 "config": {"workload": WORKLOAD, "histories_per_step": H, "global_histories": total_hist,
                            "transport": "FP32 arithmetic, FP64 tallies and energy balance",
-                           "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{world}"},
-                "fp64": {"value": fp64_value, "unit": "histories/s", "histories_per_step": FP64_HISTORIES},
+                           "job": f"{K} batches of {H} histories in one launch (batches injected back to back)",
+                           "l2": "flushed before the timed job (256 MB write); the job's batch tallies "
+                                 f"({K * prob.nreg * 8 / 1e6:.0f} MB) exceed L2",
+                           "parallelism": f"replicas x{world}"},
+                "fp64": {"value": fp64_value, "unit": "histories/s", "histories": H64 * K,
+                         "job": f"{K} batches of {H64} histories in one launch"},
                 "fp32_over_fp64": value / world / fp64_value,
                 "efficiency": {"value": efficiency, "unit": "1/(s^2*T)", "s_max_rel_above_50pct": s,
                                "T_s": dev_ms / 1000.0},
-                "latency_ms_per_step": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
-                "per_history": {"events": evs / (args.steps * H), "voxel_steps": geo / (args.steps * H),
-                                "deposits": dep / (args.steps * H), "algorithmic_bytes": per_hist_bytes},
+                "job_ms": dev_ms,
+                "per_history": {"events": evs / (K * H), "voxel_steps": geo / (K * H),
+                                "deposits": dep / (K * H), "algorithmic_bytes": per_hist_bytes},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "peak_kind": peak_kind,
-                             "traffic": (traffic_ph * H) if traffic_ph else None,
+                             "traffic": (traffic_ph * K * H) if traffic_ph else None,
                              "kernel": "wavefront_kernel<float>",
                              "atomics_per_s": dep / (dev_ms / 1000.0)},
                 "cpu_baseline": cpu,
@@ -417,20 +409,21 @@ def run_ct_leg(args, local_rank):
                 m32, m64 = a32[1:] / nb, a64[1:] / nb
                 v32 = np.maximum(b32[1:] / nb - m32 ** 2, 0) / (nb - 1)
                 v64 = np.maximum(b64[1:] / nb - m64 ** 2, 0) / (nb - 1)
-                sel = m64 > 0.2 * m64.max()
+                # Voxels are selected on the mean of both runs: selecting on one
+                # run alone picks voxels where that run fluctuated upwards.
+                mm = 0.5 * (m32 + m64)
+                sel = mm > 0.2 * mm.max()
                 tz = (m32[sel] - m64[sel]) / np.sqrt(v32[sel] + v64[sel])
                 z = S.norm.ppf(np.clip(S.t.cdf(tz, 2 * (nb - 1)), 1e-300, 1 - 1e-16))
-                hi = m64 > 0.5 * m64.max()
-                rel = (m32[hi] - m64[hi]) / m64[hi]
+                hi = mm > 0.5 * mm.max()
                 fields.append({"field": f"{gname} {2 * half:g}x{2 * half:g} cm2", "histories": H,
                                "fp32_histories_per_s": H / (s32.kernel_ms / 1e3),
                                "fp64_histories_per_s": H / (s64.kernel_ms / 1e3),
                                "voxels_above_20pct": int(sel.sum()),
                                "frac_within_2sigma": float(np.mean(np.abs(z) <= 2)),
                                "mean_z2": float(np.mean(z * z)),
-                               "mean_rel_diff_above_50pct": float(rel.mean()),
-                               "sigma_of_mean_rel_diff": float(np.sqrt(np.mean((v32[hi] + v64[hi]) / m64[hi] ** 2)
-                                                                       / hi.sum())),
+                               "dose_rel_diff_above_50pct": float(m32[hi].sum() / m64[hi].sum() - 1),
+                               "sigma_independent_voxels": float(np.sqrt((v32[hi] + v64[hi]).sum()) / m64[hi].sum()),
                                "total_energy_rel_diff": float(a32[1:].sum() / a64[1:].sum() - 1)})
     return {"metric": "FP32-transport dose error vs FP64, per field", "n_gpus": 1, "data": "synthetic",
             "config": {"workload": CT_WORKLOAD, "batches": nb}, "fields": fields}

@@ -531,9 +531,10 @@ struct SlotJob {
   int nslots;
   const long long *first;  // device [nslots+1]
   const int *beamlet;      // device [nslots] (beamlet jobs), else null
-  double *tally;           // device [nslots][nreg] (beamlet jobs), else null
+  double *tally;           // device [nslots][nreg] (beamlet and batch jobs), else null
   long long nhist;         // histories of the launch
   const void *jobs;        // device JobSlot<R>[nslots] (multi-job launches), else null
+  bool beamlets = true;    // slots are beamlets (false: batches of one job)
 };
 
 }  // namespace
@@ -558,6 +559,8 @@ struct omc_engine {
   DevBuf dij_tally, dij_first, dij_beamlet, dij_nhist, dij_max, dij_cnt, dij_off, dij_rows, dij_vals;
   // multi-job rounds
   DevBuf multi_slots, multi_first;
+  // batch tallies when all batches of a run share one launch
+  DevBuf batch_tally, batch_first;
   // per-iteration trace of the last wavefront launch (diagnostics)
   DevBuf trace;
   int trace_cap = 0;
@@ -779,6 +782,7 @@ void apply_job(Params<R> &P, const PrecisionState<R> &S, const SlotJob *job, lon
   }
   P.slot_beamlet = job->beamlet;
   P.endep = job->tally;
+  if (!job->beamlets) return;
   P.S.beamlets = 1;
   P.S.bixel = S.bixel;
   P.S.beam_src = S.beam_src;
@@ -1084,7 +1088,8 @@ extern "C" void omc_engine_destroy(omc_engine *e) {
   e->f64.beamlets.clear();
   e->f32.beamlets.clear();
   for (DevBuf *b : {&e->dij_tally, &e->dij_first, &e->dij_beamlet, &e->dij_nhist, &e->dij_max, &e->dij_cnt,
-                    &e->dij_off, &e->dij_rows, &e->dij_vals, &e->multi_slots, &e->multi_first, &e->trace})
+                    &e->dij_off, &e->dij_rows, &e->dij_vals, &e->multi_slots, &e->multi_first, &e->trace,
+                    &e->batch_tally, &e->batch_first})
     b->release();
   cudaStreamDestroy(e->stream);
   delete e;
@@ -1170,6 +1175,57 @@ extern "C" omc_status omc_engine_set_source(omc_engine *e, const omc_source *s) 
   return OMC_OK;
 }
 
+// accum = sum over batches, accum2 = sum of squares (accumEndep over
+// batch tallies kept side by side: one launch's batches, or a job's).
+__global__ void batch_accumulate_kernel(const double *tally, int nbatch, long long nreg, double *acc, double *acc2) {
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < nreg;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    double a = 0.0, a2 = 0.0;
+    for (int b = 0; b < nbatch; b++) {
+      double v = tally[static_cast<size_t>(b) * nreg + i];
+      a += v;
+      a2 += v * v;
+    }
+    acc[i] = a;
+    acc2[i] = a2;
+  }
+}
+
+static omc_status run_batches_one_launch(omc_engine *e, const omc_run_config *cfg, int nlanes, bool fp64,
+                                         omc_run_stats *stats) {
+  const int nb = cfg->nbatch;
+  omc_status s;
+  if ((s = e->batch_tally.ensure(static_cast<size_t>(nb) * e->nreg * sizeof(double))) != OMC_OK) return s;
+  if ((s = e->batch_first.ensure((nb + 1) * sizeof(long long))) != OMC_OK) return s;
+  std::vector<long long> first(nb + 1);
+  for (int b = 0; b <= nb; b++) first[b] = static_cast<long long>(b) * cfg->nperbatch;
+  CUDA_TRY(cudaMemcpyAsync(e->batch_first.p, first.data(), (nb + 1) * sizeof(long long), cudaMemcpyHostToDevice,
+                           e->stream));
+  CUDA_TRY(cudaMemsetAsync(e->batch_tally.p, 0, static_cast<size_t>(nb) * e->nreg * sizeof(double), e->stream));
+  SlotJob job{nb, static_cast<const long long *>(e->batch_first.p), nullptr, static_cast<double *>(e->batch_tally.p),
+              first[nb], nullptr, false};
+  omc_run_stats gs{};
+  s = fp64 ? run_wavefront(e, e->f64, cfg, nlanes, &gs, &job) : run_wavefront(e, e->f32, cfg, nlanes, &gs, &job);
+  if (s != OMC_OK && s != OMC_ERR_STACK && s != OMC_ERR_LIMIT) return s;
+  cudaEvent_t t0, t1;
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  cudaEventRecord(t0, e->stream);
+  batch_accumulate_kernel<<<std::max(1, static_cast<int>(std::min<long long>(4 * e->nsm, (e->nreg + 255) / 256))), 256,
+                            0, e->stream>>>(static_cast<const double *>(e->batch_tally.p), nb, e->nreg,
+                                            static_cast<double *>(e->acc.p), static_cast<double *>(e->acc2.p));
+  cudaEventRecord(t1, e->stream);
+  CUDA_TRY(cudaStreamSynchronize(e->stream));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, t0, t1);
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  gs.kernel_ms += ms;
+  gs.transport_ms += ms;
+  if (stats) *stats = gs;
+  return s;
+}
+
 // Shared start of every run: validation, schedule and lane count, RANMAR
 // streams (seeded unless continued).
 struct RunPlan {
@@ -1217,6 +1273,15 @@ static omc_status engine_run(omc_engine *e, const omc_run_config *cfg, omc_run_s
   cudaMemsetAsync(e->acc.p, 0, e->nreg * sizeof(double), e->stream);
   cudaMemsetAsync(e->acc2.p, 0, e->nreg * sizeof(double), e->stream);
   cudaMemsetAsync(e->counters.p, 0, sizeof(Counters), e->stream);
+  if (wavefront && cfg->nbatch > 1 && cfg->nbatch <= 65535) {
+    // All batches in one launch: batch b is tally slot b, histories are
+    // injected without a pause between batches, and the particles of one
+    // batch drain while the next batch is already in flight.
+    size_t fr = 0, tot = 0;
+    cudaMemGetInfo(&fr, &tot);
+    const size_t tally_bytes = static_cast<size_t>(cfg->nbatch) * e->nreg * sizeof(double);
+    if (tally_bytes <= fr * 3 / 10) return run_batches_one_launch(e, cfg, nlanes, fp64, stats);
+  }
   if (wavefront) return fp64 ? run_wavefront(e, e->f64, cfg, nlanes, stats) : run_wavefront(e, e->f32, cfg, nlanes, stats);
   return fp64 ? run_batches(e, e->f64, cfg, nlanes, depth, stats) : run_batches(e, e->f32, cfg, nlanes, depth, stats);
 }
@@ -1448,22 +1513,6 @@ struct omc_job {
 
 namespace {
 
-// accum = sum over batches, accum2 = sum of squares (accumEndep over the
-// job's batches).
-__global__ void job_accumulate_kernel(const double *tally, int nbatch, long long nreg, double *acc, double *acc2) {
-  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < nreg;
-       i += static_cast<long long>(gridDim.x) * blockDim.x) {
-    double a = 0.0, a2 = 0.0;
-    for (int b = 0; b < nbatch; b++) {
-      double v = tally[static_cast<size_t>(b) * nreg + i];
-      a += v;
-      a2 += v * v;
-    }
-    acc[i] = a;
-    acc2[i] = a2;
-  }
-}
-
 const PrecisionState<float> &job_state(const omc_job *j, float) { return j->s32; }
 const PrecisionState<double> &job_state(const omc_job *j, double) { return j->s64; }
 
@@ -1592,7 +1641,7 @@ extern "C" omc_status omc_engine_job_result(omc_engine *e, omc_job *j, double *a
   omc_status s;
   if ((s = ensure_device(e)) != OMC_OK) return s;
   double *acc = static_cast<double *>(j->result.p), *acc2 = acc + j->nreg;
-  job_accumulate_kernel<<<std::max(1, static_cast<int>(std::min<long long>(4 * e->nsm, (j->nreg + 255) / 256))), 256, 0,
+  batch_accumulate_kernel<<<std::max(1, static_cast<int>(std::min<long long>(4 * e->nsm, (j->nreg + 255) / 256))), 256, 0,
                           e->stream>>>(static_cast<const double *>(j->tally.p), j->nbatch, j->nreg, acc, acc2);
   if (accum_endep)
     CUDA_TRY(cudaMemcpyAsync(accum_endep, acc, j->nreg * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
