@@ -252,6 +252,9 @@ typedef struct omc_run_config {
                             0 = seed them from (ixx, jxx)                  */
     int schedule;        /* omc_schedule                                  */
     long long inflight;  /* wavefront: particles kept in flight, 0 = auto  */
+    int chunk_events;    /* wavefront: condensed-history steps a thread
+                            takes with one electron before it goes back to
+                            the queue; 0 = auto                           */
 } omc_run_config;
 
 typedef enum omc_schedule {
@@ -268,10 +271,17 @@ typedef struct omc_run_stats {
     long long histories;   /* histories transported                       */
     long long steps;       /* particle events processed                   */
     int max_stack;         /* deepest per-lane stack seen                 */
-    int error_flags;       /* OR of device error bits (0 = clean)         */
+    int error_flags;       /* OR of device error bits (0 = clean): 1 stack
+                              overflow, 2 sampling loop limit, 4 history
+                              event limit, 16 queue overflow, 32 grid
+                              barrier timeout                              */
     long long voxel_steps; /* geometry steps (howfar calls)               */
     long long deposits;    /* energy deposits (ausgab calls)              */
     double kernel_ms;      /* device time of the transport + batch kernels */
+    int warnings;          /* 8: an interpolation index fell outside its
+                              table and was clamped to the edge bin (rare
+                              rounding at the table ends; the reference
+                              reads outside the array there)               */
 } omc_run_stats;
 
 omc_status omc_engine_create(int device, omc_engine **out);

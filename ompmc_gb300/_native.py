@@ -62,13 +62,14 @@ class RunConfig_t(C.Structure):
     _fields_ = [("nperbatch", C.c_longlong), ("nbatch", C.c_int), ("ixx", C.c_int), ("jxx", C.c_int),
                 ("nsplit", C.c_int), ("precision", C.c_int), ("nlanes", C.c_int),
                 ("stack_depth", C.c_int), ("serial", C.c_int), ("continue_streams", C.c_int),
-                ("schedule", C.c_int), ("inflight", C.c_longlong)]
+                ("schedule", C.c_int), ("inflight", C.c_longlong), ("chunk_events", C.c_int)]
 
 
 class RunStats_t(C.Structure):
     _fields_ = [("ensrc", C.c_double), ("transport_ms", C.c_double), ("histories", C.c_longlong),
                 ("steps", C.c_longlong), ("max_stack", C.c_int), ("error_flags", C.c_int),
-                ("voxel_steps", C.c_longlong), ("deposits", C.c_longlong), ("kernel_ms", C.c_double)]
+                ("voxel_steps", C.c_longlong), ("deposits", C.c_longlong), ("kernel_ms", C.c_double),
+                ("warnings", C.c_int)]
 
 
 class Beamlets_t(C.Structure):
