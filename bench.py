@@ -210,7 +210,7 @@ def run_ours(args, rank, world, local_rank, dist_on):
         seeds = D.rank_seeds(97, 33, rank, LANES_PER_RANK_STRIDE)
         H = args.histories_per_step
         K = args.steps
-        cfg32 = api.Engine.config(H, 1, seeds=seeds, precision=api.FP32)
+        cfg32 = api.Engine.config(H, 1, seeds=seeds, precision=api.FP32, inflight=args.inflight)
         # warm-up: single batches of the same size
         for _ in range(args.warmup):
             flush_l2()
@@ -223,7 +223,8 @@ def run_ours(args, rank, world, local_rank, dist_on):
         flush_l2()
         barrier()
         sampler.start()
-        acc, acc2, st = eng.run(nperbatch=H, nbatch=K, seeds=seeds, precision=api.FP32, continue_streams=1)
+        acc, acc2, st = eng.run(nperbatch=H, nbatch=K, seeds=seeds, precision=api.FP32, continue_streams=1,
+                                inflight=args.inflight)
         barrier()
         clocks = sampler.stop()
         if st.error_flags:
@@ -530,6 +531,9 @@ def main():
     ap.add_argument("--histories-per-step", type=int, default=HISTORIES_PER_STEP,
                     help="smaller values only for profiler captures of the same code path")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--inflight", type=int, default=0,
+                    help="particles in flight (0 = the engine's default); smaller values only to keep the device "
+                         "memory of profiler captures small")
     ap.add_argument("--dij", action="store_true", help="measure the batched dij workload instead (one JSON line)")
     ap.add_argument("--dij-scale", type=float, default=1.0, help="scale of the dij history counts")
     ap.add_argument("--serve", action="store_true", help="measure the dose-server mix instead (one JSON line)")

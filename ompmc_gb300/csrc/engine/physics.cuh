@@ -55,6 +55,10 @@ struct EmitTargets {
   int *el_k;
   unsigned *el_n;
   int *ph_s, *el_s;   // tally slots [cap] (beamlet jobs only)
+  R *ei_f;            // electrons waiting for their discrete interaction
+  int *ei_k;
+  unsigned *ei_n;
+  int *ei_s;
 };
 
 __device__ __forceinline__ unsigned lanemask_lt() {
@@ -75,6 +79,8 @@ struct Lane {
   int np;    // top slot, -1 = empty (per-lane schedule)
   Particle<R> p;
   bool alive;           // wavefront: p still needs to be queued
+  bool defer_interactions = false;  // wavefront: queue discrete electron interactions
+  bool pending_interaction = false; // wavefront: p ended its step at an interaction
   EmitTargets<R> out;   // wavefront: where this phase appends
   unsigned queue_cap;
   unsigned queue_hwm;   // highest slot appended
@@ -221,6 +227,8 @@ struct Lane {
     if (q.iq == 0) emit_to(out.ph_f, out.ph_k, out.ph_n, q, out.ph_s);
     else emit_to(out.el_f, out.el_k, out.el_n, q, out.el_s);
   }
+  // The current electron, which ended its step at a discrete interaction.
+  __device__ __forceinline__ void emit_pending() { emit_to(out.ei_f, out.ei_k, out.ei_n, p, out.ei_s); }
   __device__ __forceinline__ void take(const R *f, const int *k, unsigned slot, const int *tag) {
     if (tag) set_tag(__ldcg(tag + slot));
     size_t c = queue_cap;
