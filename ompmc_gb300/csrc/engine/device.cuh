@@ -95,9 +95,33 @@ struct Tables {
 };
 
 // Voxel geometry and per-region data.
+// Unsigned division by a divisor fixed for a whole run, as a multiply-high
+// and shifts (Granlund and Montgomery, "Division by invariant integers
+// using multiplication", PLDI 1994, round-up method with a 33-bit
+// multiplier): exact for every 32-bit dividend.  l = 0 marks d = 1.
+struct InvariantDivisor {
+  unsigned m;
+  int l;
+};
+
+inline InvariantDivisor make_divisor(unsigned d) {
+  if (d <= 1) return InvariantDivisor{0u, 0};
+  int l = 0;
+  while ((1ull << l) < d) l++;  // ceil(log2 d)
+  unsigned long long m = (((1ull << 32) * ((1ull << l) - d)) / d) + 1;
+  return InvariantDivisor{static_cast<unsigned>(m), l};
+}
+
+__device__ __forceinline__ unsigned divide(unsigned n, InvariantDivisor v) {
+  if (v.l == 0) return n;
+  unsigned t = __umulhi(v.m, n);
+  return (t + ((n - t) >> 1)) >> (v.l - 1);
+}
+
 template <typename R>
 struct Geometry {
   int nx, ny, nz, nxy;
+  InvariantDivisor div_nx, div_nxy;  // region decode (omc_dosxyz.c:205-207)
   const R *xb, *yb, *zb;
   const int8_t *med;  // [nreg], -1 vacuum / outside
   const R *rhof;      // [nreg]

@@ -760,6 +760,8 @@ omc_status upload_geometry(PrecisionState<R> &S, const omc_phantom *ph, const st
   G.ny = ph->ny;
   G.nz = ph->nz;
   G.nxy = ph->nx * ph->ny;
+  G.div_nx = make_divisor(static_cast<unsigned>(ph->nx));
+  G.div_nxy = make_divisor(static_cast<unsigned>(G.nxy));
   G.xb = A.put(ph->xbounds, ph->nx + 1);
   G.yb = A.put(ph->ybounds, ph->ny + 1);
   G.zb = A.put(ph->zbounds, ph->nz + 1);

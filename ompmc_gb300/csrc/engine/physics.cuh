@@ -261,6 +261,18 @@ struct Lane {
   __device__ __forceinline__ R ecut_of(int ir) const { return __ldg(geo().ecut_m + geo().med[ir] + 1); }
   __device__ __forceinline__ R pcut_of(int ir) const { return __ldg(geo().pcut_m + geo().med[ir] + 1); }
 
+  // Voxel indices of region irl >= 1: irl = 1 + ix + iy*nx + iz*nx*ny.
+  __device__ __forceinline__ void decode(int irl, int &ix, int &iy, int &iz) const {
+    const Geometry<R> &g = geo();
+    const unsigned n = static_cast<unsigned>(irl - 1);
+    const unsigned z = divide(n, g.div_nxy);
+    const unsigned rem = n - z * static_cast<unsigned>(g.nxy);
+    const unsigned y = divide(rem, g.div_nx);
+    ix = static_cast<int>(rem - y * static_cast<unsigned>(g.nx));
+    iy = static_cast<int>(y);
+    iz = static_cast<int>(z);
+  }
+
   __device__ void howfar(const Particle<R> &q, int &idisc, int &irnew, R &ustep) {
     const Geometry<R> &g = geo();
     n_geom++;
@@ -269,9 +281,8 @@ struct Lane {
       idisc = 1;
       return;
     }
-    int irx = (irl - 1) % g.nx;
-    int irz = (irl - 1 - irx) / g.nxy;
-    int iry = ((irl - 1 - irx) - irz * g.nxy) / g.nx;
+    int irx, iry, irz;
+    decode(irl, irx, iry, irz);
     R dist;
     if (q.w > RC(0)) {
       dist = (__ldg(g.zb + irz + 1) - q.z) / q.w;
@@ -318,9 +329,8 @@ struct Lane {
     const Geometry<R> &g = geo();
     int irl = q.ir;
     if (irl == 0) return RC(0);
-    int irx = (irl - 1) % g.nx;
-    int irz = (irl - 1 - irx) / g.nxy;
-    int iry = ((irl - 1 - irx) - irz * g.nxy) / g.nx;
+    int irx, iry, irz;
+    decode(irl, irx, iry, irz);
     R t = RC(1.0E10);
     t = fmin(t, __ldg(g.xb + irx + 1) - q.x);
     t = fmin(t, q.x - __ldg(g.xb + irx));
