@@ -118,13 +118,21 @@ __device__ __forceinline__ unsigned divide(unsigned n, InvariantDivisor v) {
   return (t + ((n - t) >> 1)) >> (v.l - 1);
 }
 
+// Per-voxel transport data in one record.
+template <typename R>
+struct alignas(2 * sizeof(R)) VoxelRec {
+  R rhof;   // density / density of the medium in the pegs4 data
+  int med;  // medium index, -1 = vacuum (region 0, outside the phantom)
+};
+
 template <typename R>
 struct Geometry {
   int nx, ny, nz, nxy;
   InvariantDivisor div_nx, div_nxy;  // region decode (omc_dosxyz.c:205-207)
   const R *xb, *yb, *zb;
-  const int8_t *med;  // [nreg], -1 vacuum / outside
-  const R *rhof;      // [nreg]
+  // [nreg] voxel records {rhof, medium (-1 vacuum / outside)}: one
+  // 8-byte (FP32) or 16-byte (FP64) load per voxel visited
+  const VoxelRec<R> *vox;
   const R *ecut_m, *pcut_m;  // per medium (+1 slot for vacuum at index 0)
 };
 

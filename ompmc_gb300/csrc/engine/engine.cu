@@ -765,14 +765,18 @@ omc_status upload_geometry(PrecisionState<R> &S, const omc_phantom *ph, const st
   G.xb = A.put(ph->xbounds, ph->nx + 1);
   G.yb = A.put(ph->ybounds, ph->ny + 1);
   G.zb = A.put(ph->zbounds, ph->nz + 1);
-  G.rhof = A.put(rhof.data(), rhof.size());
   G.ecut_m = A.put(ecut_m, nmed + 1);
   G.pcut_m = A.put(pcut_m, nmed + 1);
-  DevBuf mb;
-  if (mb.ensure(med.size()) != OMC_OK) return OMC_ERR_NOMEM;
-  cudaMemcpy(mb.p, med.data(), med.size(), cudaMemcpyHostToDevice);
-  A.bufs.push_back(mb);
-  G.med = static_cast<const int8_t *>(mb.p);
+  std::vector<VoxelRec<R>> vox(med.size());
+  for (size_t i = 0; i < med.size(); i++) {
+    vox[i].rhof = static_cast<R>(rhof[i]);
+    vox[i].med = med[i];
+  }
+  DevBuf vb;
+  if (vb.ensure(vox.size() * sizeof(VoxelRec<R>)) != OMC_OK) return OMC_ERR_NOMEM;
+  cudaMemcpy(vb.p, vox.data(), vox.size() * sizeof(VoxelRec<R>), cudaMemcpyHostToDevice);
+  A.bufs.push_back(vb);
+  G.vox = static_cast<const VoxelRec<R> *>(vb.p);
   for (auto &b : A.bufs)
     if (!b.p) return fail(OMC_ERR_NOMEM, "geometry upload failed");
   S.geom_ok = true;

@@ -38,6 +38,16 @@ __device__ __forceinline__ V4<double> ld4(const V4<double> *p) {
   return V4<double>{a.x, a.y, b.x, b.y};
 }
 
+// One vector load per voxel record.
+__device__ __forceinline__ VoxelRec<float> load_voxel(const VoxelRec<float> *p) {
+  float2 v = __ldg(reinterpret_cast<const float2 *>(p));
+  return VoxelRec<float>{v.x, __float_as_int(v.y)};
+}
+__device__ __forceinline__ VoxelRec<double> load_voxel(const VoxelRec<double> *p) {
+  double2 v = __ldg(reinterpret_cast<const double2 *>(p));
+  return VoxelRec<double>{v.x, static_cast<int>(__double_as_longlong(v.y))};
+}
+
 // Separately rounded products and sums (never fused into an FMA), where a
 // one-ulp difference from the reference's arithmetic matters.
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
@@ -256,10 +266,11 @@ struct Lane {
   }
 
   // ---- geometry: region decode, howfar, hownear (omc_dosxyz.c:187-334) ----
-  __device__ __forceinline__ int med_of(int ir) const { return geo().med[ir]; }
-  __device__ __forceinline__ R rhof_of(int ir) const { return __ldg(geo().rhof + ir); }
-  __device__ __forceinline__ R ecut_of(int ir) const { return __ldg(geo().ecut_m + geo().med[ir] + 1); }
-  __device__ __forceinline__ R pcut_of(int ir) const { return __ldg(geo().pcut_m + geo().med[ir] + 1); }
+  __device__ __forceinline__ VoxelRec<R> voxel(int ir) const { return load_voxel(geo().vox + ir); }
+  __device__ __forceinline__ int med_of(int ir) const { return voxel(ir).med; }
+  __device__ __forceinline__ R rhof_of(int ir) const { return voxel(ir).rhof; }
+  __device__ __forceinline__ R ecut_of(int ir) const { return __ldg(geo().ecut_m + med_of(ir) + 1); }
+  __device__ __forceinline__ R pcut_of(int ir) const { return __ldg(geo().pcut_m + med_of(ir) + 1); }
 
   // Voxel indices of region irl >= 1: irl = 1 + ix + iy*nx + iz*nx*ny.
   __device__ __forceinline__ void decode(int irl, int &ix, int &iy, int &iz) const {
