@@ -35,6 +35,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function", f"-I{INCLUDE}"]
 NVCCFLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", f"-I{INCLUDE}",
                     "-Xptxas", "-warn-spills", "--expt-relaxed-constexpr"]
+# Extra -D definitions for tuning builds (e.g. OMC_NVCC_DEFINES="OMC_MIN_BLOCKS_FP32=5").
+NVCCFLAGS += [f"-D{d}" for d in os.environ.get("OMC_NVCC_DEFINES", "").split() if d]
 
 
 def _nvcc():
