@@ -271,30 +271,35 @@ __global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) wavefront_ke
     // Everything produced goes to the next iteration's queues.
     L.out = EmitTargets<R>{W.ph_f[bout], W.ph_k[bout], W.ctr + cout, W.el_f[bout], W.el_k[bout], W.ctr + 3 + cout,
                            W.ph_s[bout], W.el_s[bout], W.ei_f[bout], W.ei_k[bout], W.ctr + 6 + cout, W.ei_s[bout]};
-    const unsigned long long m_pad = (static_cast<unsigned long long>(m) + 31) & ~31ull;
-    const unsigned long long ph_pad = (static_cast<unsigned long long>(n_ph) + 31) & ~31ull;
+    // Chunk ranges of the phase in claim order [new histories | photons |
+    // electron steps | electron interactions], each but the last padded to
+    // a multiple of 32 so that a warp's chunk is one code path.  (Claiming
+    // the electron steps first, largest work first, measured 3% slower.)
     const unsigned long long el_pad = (static_cast<unsigned long long>(n_el) + 31) & ~31ull;
-    const unsigned long long total = m_pad + ph_pad + el_pad + n_ei;
+    const unsigned long long ph_pad = (static_cast<unsigned long long>(n_ph) + 31) & ~31ull;
+    const unsigned long long r_in = 0, r_ph = r_in + ((static_cast<unsigned long long>(m) + 31) & ~31ull),
+                             r_el = r_ph + ph_pad, r_ei = r_el + el_pad, total = r_ei + n_ei;
     for (;;) {
       unsigned long long base = 0;
       if (lane_id == 0) base = atomicAdd(W.work + cin, 32ull);
       base = __shfl_sync(0xffffffffu, base, 0);
       if (base >= total) break;
       const unsigned long long i = base + lane_id;
-      if (base < m_pad) {
-        if (i < static_cast<unsigned long long>(m)) {
-          L.init_history(static_cast<long long>(injected + i));
+      if (base >= r_in && base < r_in + ((static_cast<unsigned long long>(m) + 31) & ~31ull)) {
+        const unsigned long long k = i - r_in;
+        if (k < static_cast<unsigned long long>(m)) {
+          L.init_history(static_cast<long long>(injected + k));
           L.emit(L.p);
         }
-      } else if (base < m_pad + ph_pad) {
-        const unsigned long long k = i - m_pad;
+      } else if (base >= r_ph && base < r_ph + ph_pad) {
+        const unsigned long long k = i - r_ph;
         if (k < n_ph) {
           L.take(W.ph_f[bin], W.ph_k[bin], static_cast<unsigned>(k), W.ph_s[bin]);
           L.wf_photon_event();
           events++;
         }
-      } else if (base < m_pad + ph_pad + el_pad) {
-        const unsigned long long k = i - m_pad - ph_pad;
+      } else if (base >= r_el && base < r_el + el_pad) {
+        const unsigned long long k = i - r_el;
         if (k < n_el) {
           // Up to chunk_events iterations of electron()'s tstep loop on
           // this electron; it goes back to a queue if it is still alive
@@ -313,7 +318,7 @@ __global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) wavefront_ke
           }
         }
       } else {
-        const unsigned long long k = i - m_pad - ph_pad - el_pad;
+        const unsigned long long k = i - r_ei;
         if (k < n_ei) {
           L.take(W.ei_f[bin], W.ei_k[bin], static_cast<unsigned>(k), W.ei_s[bin]);
           L.deferred_interaction();
