@@ -367,6 +367,39 @@ def run_dij_leg(args, local_rank):
         return line
 
 
+def run_vrt_leg(args, local_rank):
+    """Photon splitting (the reference's only variance reduction, "nsplit")
+    on the benchmark workload: efficiency 1/(s^2 T) of a 10-batch FP32 job
+    per splitting number, s from the job's own batches."""
+    import torch
+
+    from ompmc_gb300 import api
+
+    torch.cuda.set_device(local_rank)
+    H = args.vrt_histories
+    out = []
+    with tempfile.TemporaryDirectory() as tmp:
+        prob = build_problem(tmp)
+        eng = api.Engine(local_rank).load(prob)
+        eng.run(nperbatch=H // 10, nbatch=2, precision=api.FP32)
+        for ns in (1, 2, 4, 8, 16, 32):
+            acc, acc2, st = eng.run(nperbatch=H, nbatch=10, nsplit=ns, precision=api.FP32, seeds=(97, 33 + ns))
+            if st.error_flags:
+                raise RuntimeError(f"device error flags {st.error_flags:#x} at nsplit {ns}")
+            m, m2 = acc[1:] / 10, acc2[1:] / 10
+            sel = m > 0.5 * m.max()
+            rel = np.sqrt(np.maximum(m2[sel] - m[sel] ** 2, 0.0) / 9) / m[sel]
+            T = st.kernel_ms / 1e3
+            out.append({"nsplit": ns, "histories_per_s": 10 * H / T, "T_s": T, "s_max": float(rel.max()),
+                        "s_mean": float(rel.mean()), "efficiency_max": float(1 / (rel.max() ** 2 * T)),
+                        "efficiency_mean": float(1 / (rel.mean() ** 2 * T))})
+        eng.close()
+    return {"metric": "efficiency 1/(s^2 T) vs photon splitting", "n_gpus": 1, "data": "synthetic",
+            "config": {"workload": WORKLOAD, "histories": 10 * H, "batches": 10,
+                       "s": "relative batch sigma over voxels above 50% of Dmax (max and mean)"},
+            "results": out}
+
+
 CT_WORKLOAD = ("CT-like blob phantom 256x256x128 @ 2 mm (seed 2024), synthetic 6 MV, point source SSD 100 cm; "
                "fields 3x3 and 10x10 cm2 at gantry 0 (+z) and gantry 90 (phantom axes x and z exchanged so that "
                "the beam enters along +z)")
@@ -538,6 +571,8 @@ def main():
     ap.add_argument("--dij-scale", type=float, default=1.0, help="scale of the dij history counts")
     ap.add_argument("--serve", action="store_true", help="measure the dose-server mix instead (one JSON line)")
     ap.add_argument("--ct", action="store_true", help="FP32-vs-FP64 dose error per field on the CT-like phantom")
+    ap.add_argument("--vrt", action="store_true", help="efficiency 1/(s^2 T) against the photon splitting number")
+    ap.add_argument("--vrt-histories", type=int, default=2_000_000, help="histories per batch (10 batches)")
     ap.add_argument("--ct-histories", type=int, default=20_000_000)
     ap.add_argument("--serve-jobs", type=int, default=40)
     ap.add_argument("--serve-rate", type=float, default=0.5, help="job arrivals per second")
@@ -555,6 +590,10 @@ def main():
     if args.dij:
         if rank == 0:
             print(json.dumps(run_dij_leg(args, local_rank)), flush=True)
+        return
+    if args.vrt:
+        if rank == 0:
+            print(json.dumps(run_vrt_leg(args, local_rank)), flush=True)
         return
     if args.ct:
         if rank == 0:
