@@ -301,6 +301,18 @@ omc_status omc_engine_set_source(omc_engine *e, const omc_source *s);
 omc_status omc_engine_run(omc_engine *e, const omc_run_config *cfg,
                           double *accum_endep, double *accum_endep2,
                           omc_run_stats *stats);
+/* Autotuner of the wavefront run options for the loaded geometry and
+ * source: times one-launch runs of sample_histories (2 batches) for every
+ * in-flight target of 32, 64, 128 and 192 particles per thread and 1 or 2
+ * electron steps per queue take, at cfg's precision and splitting, and
+ * writes the fastest into *best (a copy of *cfg with inflight and
+ * chunk_events set).  rates (may be NULL) receives the histories/s of the
+ * 8 candidates in that order.  The RANMAR streams are left where the last
+ * trial ended; seed them for the production run. */
+omc_status omc_engine_tune(omc_engine *e, const omc_run_config *cfg,
+                           long long sample_histories, omc_run_config *best,
+                           double *rates);
+
 /* Same, leaving the tallies on the device; returns device pointers valid
  * until the next run (for resident pipelines and benchmarks). */
 omc_status omc_engine_run_resident(omc_engine *e, const omc_run_config *cfg,

@@ -260,6 +260,17 @@ class Engine:
         col_ptr, rows, vals = _take_dij(out, fp32_values)
         return col_ptr, rows, vals, st
 
+    def tune(self, precision=FP32, sample_histories=2_000_000, nsplit=None, seeds=None):
+        """omc_engine_tune: (inflight, chunk_events, rates of the 8
+        candidates) fastest for the loaded geometry and source."""
+        p = self._problem
+        cfg = self.config(2, 2, p.seeds if seeds is None else seeds, p.nsplit if nsplit is None else nsplit,
+                          precision)
+        best = N.RunConfig_t()
+        rates = (C.c_double * 8)()
+        check(N.lib().omc_engine_tune(self._h, C.byref(cfg), int(sample_histories), C.byref(best), rates))
+        return int(best.inflight), int(best.chunk_events), list(rates)
+
     def trace(self, iterations):
         """Record per-iteration device time and queue sizes of the next
         wavefront launches (0 = off)."""

@@ -1357,6 +1357,40 @@ extern "C" omc_status omc_engine_run(omc_engine *e, const omc_run_config *cfg, d
   return s;
 }
 
+extern "C" omc_status omc_engine_tune(omc_engine *e, const omc_run_config *cfg, long long sample_histories,
+                                      omc_run_config *best, double *rates) {
+  if (!e || !cfg || !best) return fail(OMC_ERR_ARG, "null argument");
+  if (sample_histories < 2) return fail(OMC_ERR_ARG, "sample_histories must be >= 2");
+  RunPlan rp;
+  omc_run_config probe = *cfg;
+  probe.schedule = OMC_SCHEDULE_WAVEFRONT;
+  probe.serial = 0;
+  probe.nbatch = 2;
+  probe.nperbatch = sample_histories / 2;
+  omc_status s = prepare_run(e, &probe, rp);  // seeds the streams once
+  if (s != OMC_OK) return s;
+  probe.continue_streams = 1;
+  static const int per_thread[4] = {32, 64, 128, 192};
+  double best_rate = -1.0;
+  *best = *cfg;
+  for (int k = 0; k < 8; k++) {
+    probe.inflight = static_cast<long long>(rp.nlanes) * per_thread[k / 2];
+    probe.chunk_events = 1 + k % 2;
+    omc_run_stats st{};
+    s = engine_run(e, &probe, &st);
+    if (s != OMC_OK) return s;
+    double rate = st.kernel_ms > 0 ? static_cast<double>(probe.nperbatch * probe.nbatch) / (st.kernel_ms * 1e-3) : 0;
+    if (rates) rates[k] = rate;
+    if (rate > best_rate) {
+      best_rate = rate;
+      best->inflight = probe.inflight;
+      best->chunk_events = probe.chunk_events;
+      best->schedule = OMC_SCHEDULE_WAVEFRONT;
+    }
+  }
+  return OMC_OK;
+}
+
 extern "C" omc_status omc_engine_run_resident(omc_engine *e, const omc_run_config *cfg, const double **d_acc,
                                               const double **d_acc2, omc_run_stats *stats) {
   omc_status s = engine_run(e, cfg, stats);
