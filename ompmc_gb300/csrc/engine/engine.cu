@@ -364,52 +364,76 @@ constexpr int kDijThreads = 256;
 constexpr int kDijRounds = 16;
 constexpr int kDijTile = kDijThreads * kDijRounds;
 
-__device__ __forceinline__ double block_max(double v, double *red) {
-  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-  }
-  return v;
-}
-
-// Energy to Gy per history, in the reference's operation order:
-// (sum / nbatch) * (1.602e-10 / (dx*dy*dz*rho * nhist)); zero below
-// 0.044 g/cm^3.  Grid: x over voxels, y over slots.
-__global__ void dij_dose_kernel(double *tally, long long nreg, int nx, int ny, const double *xb, const double *yb,
-                                const double *zb, const double *density, const double *slot_nhist, int nbatch,
-                                unsigned long long *slot_max) {
-  __shared__ double red[32];
-  const int s = blockIdx.y;
-  double *t = tally + static_cast<size_t>(s) * nreg + 1;
-  const double nh = slot_nhist[s];
-  const long long nvox = nreg - 1;
-  double m = 0.0;
+// Per-voxel dose factor, once per tally group, in the reference's
+// operation order (omc_matrad.c:868-882): mass = dx*dy*dz*rho, factor =
+// 1.602e-10 / (mass * nhist) when every beamlet of the group has nhist
+// histories, else 1.602e-10 / mass (the beamlet's 1/nhist is applied per
+// element); zero below 0.044 g/cm^3, where the reference zeroes the dose.
+__global__ void dij_factor_kernel(long long nvox, int nx, int ny, const double *xb, const double *yb, const double *zb,
+                                  const double *density, double nhist, double *factor) {
   for (long long v = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; v < nvox;
        v += static_cast<long long>(gridDim.x) * blockDim.x) {
     const int ix = static_cast<int>(v % nx);
     const long long r = v / nx;
     const int iy = static_cast<int>(r % ny);
     const int iz = static_cast<int>(r / ny);
-    double endep = __ddiv_rn(t[v], static_cast<double>(nbatch));
     double mass = __dmul_rn(__dmul_rn(__dsub_rn(xb[ix + 1], xb[ix]), __dsub_rn(yb[iy + 1], yb[iy])),
                             __dsub_rn(zb[iz + 1], zb[iz]));
     const double rho = density[v];
     mass = __dmul_rn(mass, rho);
-    endep = __dmul_rn(endep, __ddiv_rn(1.602E-10, __dmul_rn(mass, nh)));
-    if (rho < 0.044) endep = 0.0;
-    t[v] = endep;
-    m = fmax(m, endep);
+    double f = nhist > 0.0 ? __ddiv_rn(1.602E-10, __dmul_rn(mass, nhist)) : __ddiv_rn(1.602E-10, mass);
+    if (rho < 0.044) f = 0.0;
+    factor[v] = f;
   }
-  m = block_max(m, red);
-  // Non-negative doubles order like their bit patterns.
-  if (threadIdx.x == 0) atomicMax(slot_max + s, static_cast<unsigned long long>(__double_as_longlong(m)));
 }
 
-__device__ __forceinline__ double slot_threshold(const unsigned long long *slot_max, int s, double rel) {
-  return __dmul_rn(__longlong_as_double(static_cast<long long>(slot_max[s])), rel);
+// Energy to dose in place, (sum / nbatch) * factor, and each slot's
+// maximum.  Grid: x over voxels, y over slots.  When the beamlets of the
+// group have different history counts, the factor leaves out 1/nhist: it
+// is a positive constant of the slot, so the maximum and the threshold
+// test are taken on the unscaled values and only the kept entries are
+// scaled (dij_fill_kernel), one FP64 multiply per entry instead of one per
+// voxel.
+__global__ void dij_dose_kernel(double *__restrict__ tally, long long nreg, const double *__restrict__ factor,
+                                int nbatch, unsigned long long *__restrict__ slot_max) {
+  const int s = blockIdx.y;
+  double *__restrict__ t = tally + static_cast<size_t>(s) * nreg + 1;
+  const long long nvox = nreg - 1;
+  const double nb = static_cast<double>(nbatch);
+  // The maximum is taken on the bit patterns as signed 64-bit integers
+  // (non-negative doubles order like their bits; -0.0 and negative values
+  // fall below every non-negative one): the FP64 pipe of this GPU is narrow
+  // and the conversion itself has to use it.  Four independent elements
+  // per thread and round keep several loads in flight.
+  long long m = 0;
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long v0 = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; v0 < nvox; v0 += 4 * stride) {
+    double e[4], f[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const long long v = v0 + k * stride;
+      e[k] = v < nvox ? t[v] : 0.0;
+      f[k] = v < nvox ? __ldg(factor + v) : 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const long long v = v0 + k * stride;
+      if (v >= nvox) break;
+      double endep = e[k];
+      if (nbatch != 1) endep = __ddiv_rn(endep, nb);
+      endep = __dmul_rn(endep, f[k]);
+      t[v] = endep;
+      m = max(m, __double_as_longlong(endep));
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0 && m > 0) atomicMax(slot_max + s, static_cast<unsigned long long>(m));
+}
+
+// The threshold of slot s as the bit pattern of a non-negative double:
+// t > threshold compares as signed 64-bit integers (see dij_dose_kernel).
+__device__ __forceinline__ long long slot_threshold(const unsigned long long *slot_max, int s, double rel) {
+  return __double_as_longlong(__dmul_rn(__longlong_as_double(static_cast<long long>(slot_max[s])), rel));
 }
 
 // Entries above the threshold per tile.  Grid: x over tiles, y over slots.
@@ -417,8 +441,8 @@ __global__ void dij_count_kernel(const double *tally, long long nreg, int ntiles
                                  double rel, long long *tile_count) {
   __shared__ int red[kDijThreads / 32];
   const int s = blockIdx.y;
-  const double thresh = slot_threshold(slot_max, s, rel);
-  const double *t = tally + static_cast<size_t>(s) * nreg + 1;
+  const long long thresh = slot_threshold(slot_max, s, rel);
+  const long long *t = reinterpret_cast<const long long *>(tally + static_cast<size_t>(s) * nreg + 1);
   const long long nvox = nreg - 1;
   const long long v0 = static_cast<long long>(blockIdx.x) * kDijTile;
   int c = 0;
@@ -463,10 +487,12 @@ __global__ void dij_scan_kernel(const long long *cnt, long long n, long long *of
 // Rows (voxel index = region - 1) and values of the kept entries, in voxel
 // order within each slot.
 __global__ void dij_fill_kernel(const double *tally, long long nreg, int ntiles, const unsigned long long *slot_max,
-                                double rel, const long long *off, int *rows, double *vals, float *vals32) {
+                                double rel, const long long *off, const double *slot_inv_nhist, int *rows,
+                                double *vals, float *vals32) {
   __shared__ int wtot[kDijThreads / 32];
   const int s = blockIdx.y;
-  const double thresh = slot_threshold(slot_max, s, rel);
+  const double inv_nh = slot_inv_nhist ? slot_inv_nhist[s] : 1.0;
+  const long long thresh = slot_threshold(slot_max, s, rel);
   const double *t = tally + static_cast<size_t>(s) * nreg + 1;
   const long long nvox = nreg - 1;
   const long long v0 = static_cast<long long>(blockIdx.x) * kDijTile;
@@ -478,7 +504,7 @@ __global__ void dij_fill_kernel(const double *tally, long long nreg, int ntiles,
     bool keep = false;
     if (v < nvox) {
       d = t[v];
-      keep = d > thresh;
+      keep = __double_as_longlong(d) > thresh;
     }
     const unsigned m = __ballot_sync(0xffffffffu, keep);
     if (lane == 0) wtot[warp] = __popc(m);
@@ -491,6 +517,7 @@ __global__ void dij_fill_kernel(const double *tally, long long nreg, int ntiles,
     }
     if (keep) {
       const long long o = base + wbase + __popc(m & lanemask_lt());
+      if (slot_inv_nhist) d = __dmul_rn(d, inv_nh);
       rows[o] = static_cast<int>(v);
       if (vals) vals[o] = d;
       else vals32[o] = static_cast<float>(d);
@@ -601,7 +628,7 @@ struct omc_engine {
   DevBuf density;
   int nbeamlets = 0, nbeams = 0;
   // beamlet-job buffers
-  DevBuf dij_tally, dij_first, dij_beamlet, dij_nhist, dij_max, dij_cnt, dij_off, dij_rows, dij_vals;
+  DevBuf dij_tally, dij_first, dij_beamlet, dij_nhist, dij_max, dij_cnt, dij_off, dij_rows, dij_vals, dij_factor;
   // multi-job rounds
   DevBuf multi_slots, multi_first;
   // batch tallies when all batches of a run share one launch
@@ -1151,7 +1178,7 @@ extern "C" void omc_engine_destroy(omc_engine *e) {
   e->f32.beamlets.clear();
   for (DevBuf *b : {&e->dij_tally, &e->dij_first, &e->dij_beamlet, &e->dij_nhist, &e->dij_max, &e->dij_cnt,
                     &e->dij_off, &e->dij_rows, &e->dij_vals, &e->multi_slots, &e->multi_first, &e->trace,
-                    &e->batch_tally, &e->batch_first})
+                    &e->batch_tally, &e->batch_first, &e->dij_factor})
     b->release();
   cudaStreamDestroy(e->stream);
   delete e;
@@ -1478,6 +1505,7 @@ omc_status run_dij(omc_engine *e, const omc_run_config *cfg, const omc_dij_confi
   if ((s = e->dij_max.ensure(G * sizeof(unsigned long long))) != OMC_OK) return s;
   if ((s = e->dij_cnt.ensure(static_cast<size_t>(G) * ntiles * sizeof(long long))) != OMC_OK) return s;
   if ((s = e->dij_off.ensure((static_cast<size_t>(G) * ntiles + 1) * sizeof(long long))) != OMC_OK) return s;
+  if ((s = e->dij_factor.ensure(static_cast<size_t>(nvox) * sizeof(double))) != OMC_OK) return s;
 
   out->nrows = static_cast<int>(nvox);
   out->ncols = nb;
@@ -1499,7 +1527,7 @@ omc_status run_dij(omc_engine *e, const omc_run_config *cfg, const omc_dij_confi
     for (int i = 0; i < ng; i++) {
       first[i + 1] = first[i] + nh[g0 + i];
       bl[i] = g0 + i;
-      nhd[i] = static_cast<double>(nh[g0 + i]);
+      nhd[i] = 1.0 / static_cast<double>(nh[g0 + i]);  // per-slot 1/nhist (uneven counts)
     }
     cudaMemcpyAsync(e->dij_first.p, first.data(), (ng + 1) * sizeof(long long), cudaMemcpyHostToDevice, e->stream);
     cudaMemcpyAsync(e->dij_beamlet.p, bl.data(), ng * sizeof(int), cudaMemcpyHostToDevice, e->stream);
@@ -1518,15 +1546,21 @@ omc_status run_dij(omc_engine *e, const omc_run_config *cfg, const omc_dij_confi
     if (s != OMC_OK && s != OMC_ERR_STACK && s != OMC_ERR_LIMIT) return s;
     if (s != OMC_OK) worst = s;
     // Dose, threshold, compaction.
-    const int bx = static_cast<int>(std::min<long long>((nvox + 255) / 256, std::max(1, 8 * e->nsm / ng + 1)));
     double *tally = static_cast<double *>(e->dij_tally.p);
     auto *smax = static_cast<unsigned long long *>(e->dij_max.p);
     auto *cnt = static_cast<long long *>(e->dij_cnt.p);
     auto *off = static_cast<long long *>(e->dij_off.p);
-    dij_dose_kernel<<<dim3(bx, ng), 256, 0, e->stream>>>(tally, nreg, e->f64.G.nx, e->f64.G.ny, xb, yb, zb,
-                                                         static_cast<const double *>(e->density.p),
-                                                         static_cast<const double *>(e->dij_nhist.p), cfg->nbatch,
-                                                         smax);
+    // Per-voxel factor; the group's history count goes into it when every
+    // beamlet of the group has the same count (the reference's case, bit
+    // for bit), else each slot applies its own 1/nhist.
+    bool uniform = true;
+    for (int i = 1; i < ng; i++) uniform = uniform && nh[g0 + i] == nh[g0];
+    double *factor = static_cast<double *>(e->dij_factor.p);
+    dij_factor_kernel<<<static_cast<int>(std::min<long long>((nvox + 255) / 256, 16 * e->nsm)), 256, 0, e->stream>>>(
+        nvox, e->f64.G.nx, e->f64.G.ny, xb, yb, zb, static_cast<const double *>(e->density.p),
+        uniform ? static_cast<double>(nh[g0]) : 0.0, factor);
+    const int bx = static_cast<int>(std::min<long long>((nvox + 255) / 256, std::max(4, 64 * e->nsm / ng + 1)));
+    dij_dose_kernel<<<dim3(bx, ng), 256, 0, e->stream>>>(tally, nreg, factor, cfg->nbatch, smax);
     dij_count_kernel<<<dim3(ntiles, ng), kDijThreads, 0, e->stream>>>(tally, nreg, ntiles, smax, dc->rel_threshold,
                                                                       cnt);
     const long long ncnt = static_cast<long long>(ng) * ntiles;
@@ -1537,7 +1571,8 @@ omc_status run_dij(omc_engine *e, const omc_run_config *cfg, const omc_dij_confi
     if ((s = e->dij_rows.ensure((gnnz ? gnnz : 1) * sizeof(int))) != OMC_OK) return s;
     if ((s = e->dij_vals.ensure((gnnz ? gnnz : 1) * vsize)) != OMC_OK) return s;
     dij_fill_kernel<<<dim3(ntiles, ng), kDijThreads, 0, e->stream>>>(
-        tally, nreg, ntiles, smax, dc->rel_threshold, off, static_cast<int *>(e->dij_rows.p),
+        tally, nreg, ntiles, smax, dc->rel_threshold, off,
+        uniform ? nullptr : static_cast<const double *>(e->dij_nhist.p), static_cast<int *>(e->dij_rows.p),
         f32v ? nullptr : static_cast<double *>(e->dij_vals.p), f32v ? static_cast<float *>(e->dij_vals.p) : nullptr);
     // Column starts: the offset of each slot's first tile.
     CUDA_TRY(cudaMemcpy2DAsync(tile0.data(), sizeof(long long), off, static_cast<size_t>(ntiles) * sizeof(long long),
