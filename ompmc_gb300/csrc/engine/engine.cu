@@ -162,8 +162,12 @@ struct Wavefront {
   R *ei_f[2];             // electrons waiting for a discrete interaction
   int *ei_k[2];
   int *ei_s[2];
+  R *pi_f[2];             // photons waiting for their interaction
+  int *pi_k[2];
+  int *pi_s[2];
   unsigned cap;           // slots per queue
-  unsigned *ctr;          // [0..2] photon, [3..5] electron, [6..8] interaction counters
+  unsigned *ctr;          // [0..2] photon, [3..5] electron, [6..8] electron-interaction,
+                          // [9..11] photon-interaction counters
   unsigned long long *work;      // [3] chunk counters of the phase
   unsigned long long *injected;  // [2] histories injected before the iteration
   unsigned *bar_arrive;
@@ -230,8 +234,9 @@ __global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) wavefront_ke
   L.rng.j = P.rng_ijc[P.nlanes + gtid];
   L.rng.c = P.rng_ijc[2 * P.nlanes + gtid];
   L.queue_cap = W.cap;
-  // Discrete electron interactions run in their own chunks (measured on
-  // the 6 MV slab: FP32 2.85e7 -> 3.10e7, FP64 2.02e6 -> 2.22e6 hist/s).
+  // Photon and discrete electron interactions run in their own chunks
+  // (measured on the 6 MV slab: electrons FP32 2.85e7 -> 3.10e7 and FP64
+  // 2.02e6 -> 2.22e6 hist/s; photons then 3.96e7 -> 4.29e7).
   L.defer_interactions = true;
   unsigned long long events = 0;
   int it = 0;
@@ -243,9 +248,10 @@ __global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) wavefront_ke
     const unsigned n_ph = vload(W.ctr + cin);
     const unsigned n_el = vload(W.ctr + 3 + cin);
     const unsigned n_ei = vload(W.ctr + 6 + cin);
+    const unsigned n_pi = vload(W.ctr + 9 + cin);
     const unsigned long long injected = *static_cast<volatile unsigned long long *>(W.injected + bin);
     const long long remaining = P.nhist - static_cast<long long>(injected);
-    const unsigned long long inflight = static_cast<unsigned long long>(n_ph) + n_el + n_ei;
+    const unsigned long long inflight = static_cast<unsigned long long>(n_ph) + n_el + n_ei + n_pi;
     if (W.trace && gtid == 0 && it < W.trace_cap) {
       unsigned long long ns;
       asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(ns));
@@ -263,22 +269,29 @@ __global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) wavefront_ke
       W.ctr[cfree] = 0;
       W.ctr[3 + cfree] = 0;
       W.ctr[6 + cfree] = 0;
+      W.ctr[9 + cfree] = 0;
       W.work[cfree] = 0;
       W.injected[bout] = injected + static_cast<unsigned long long>(m);
     }
     // One phase: new histories, then photons, then electrons, each range
     // padded to a multiple of 32 so that a warp's chunk is one code path.
     // Everything produced goes to the next iteration's queues.
-    L.out = EmitTargets<R>{W.ph_f[bout], W.ph_k[bout], W.ctr + cout, W.el_f[bout], W.el_k[bout], W.ctr + 3 + cout,
-                           W.ph_s[bout], W.el_s[bout], W.ei_f[bout], W.ei_k[bout], W.ctr + 6 + cout, W.ei_s[bout]};
-    // Chunk ranges of the phase in claim order [new histories | photons |
-    // electron steps | electron interactions], each but the last padded to
-    // a multiple of 32 so that a warp's chunk is one code path.  (Claiming
-    // the electron steps first, largest work first, measured 3% slower.)
+    L.out = EmitTargets<R>{W.ph_f[bout], W.ph_k[bout], W.ctr + cout,     W.el_f[bout], W.el_k[bout],
+                           W.ctr + 3 + cout, W.ph_s[bout], W.el_s[bout],     W.ei_f[bout], W.ei_k[bout],
+                           W.ctr + 6 + cout, W.ei_s[bout], W.pi_f[bout],     W.pi_k[bout], W.ctr + 9 + cout,
+                           W.pi_s[bout]};
+    // Chunk ranges of the phase in claim order [new histories | photon
+    // flights | photon interactions | electron steps | electron
+    // interactions], each padded to a multiple of 32 so that a warp's chunk
+    // is one code path.  (Claiming the electron steps first, largest work
+    // first, measured 3% slower.)
     const unsigned long long el_pad = (static_cast<unsigned long long>(n_el) + 31) & ~31ull;
     const unsigned long long ph_pad = (static_cast<unsigned long long>(n_ph) + 31) & ~31ull;
+    const unsigned long long pi_pad = (static_cast<unsigned long long>(n_pi) + 31) & ~31ull;
+    const unsigned long long ei_pad = (static_cast<unsigned long long>(n_ei) + 31) & ~31ull;
     const unsigned long long r_in = 0, r_ph = r_in + ((static_cast<unsigned long long>(m) + 31) & ~31ull),
-                             r_el = r_ph + ph_pad, r_ei = r_el + el_pad, total = r_ei + n_ei;
+                             r_pi = r_ph + ph_pad, r_el = r_pi + pi_pad, r_ei = r_el + el_pad,
+                             total = r_ei + ei_pad;
     for (;;) {
       unsigned long long base = 0;
       if (lane_id == 0) base = atomicAdd(W.work + cin, 32ull);
@@ -297,6 +310,14 @@ __global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) wavefront_ke
           L.take(W.ph_f[bin], W.ph_k[bin], static_cast<unsigned>(k), W.ph_s[bin]);
           L.wf_photon_event();
           events++;
+        }
+      } else if (base >= r_pi && base < r_pi + pi_pad) {
+        const unsigned long long k = i - r_pi;
+        if (k < n_pi) {
+          L.take(W.pi_f[bin], W.pi_k[bin], static_cast<unsigned>(k), W.pi_s[bin]);
+          const bool survivor = L.p.iq == 2;
+          L.p.iq = 0;
+          L.deferred_photon_interaction(survivor);
         }
       } else if (base >= r_el && base < r_el + el_pad) {
         const unsigned long long k = i - r_el;
@@ -968,7 +989,7 @@ omc_status run_batches(omc_engine *e, PrecisionState<R> &S, const omc_run_config
 }
 
 struct WfCounters {
-  unsigned ctr[9];
+  unsigned ctr[12];
   unsigned long long work[3];
   unsigned long long injected[2];
   unsigned bar_arrive, bar_gen;
@@ -1002,7 +1023,7 @@ omc_status run_wavefront(omc_engine *e, PrecisionState<R> &S, const omc_run_conf
   if (cap > 0x7fffffffull) cap = 0x7fffffffull;
   const size_t tag_bytes = job ? static_cast<size_t>(cap) * sizeof(int) : 0;
   size_t per_queue = static_cast<size_t>(cap) * (8 * sizeof(R) + sizeof(int)) + tag_bytes;
-  const int nqueues = 6;  // photons, electrons, interactions; two generations each
+  const int nqueues = 8;  // photons, electrons, electron and photon interactions; two generations each
   if (S.queue.ensure(nqueues * per_queue) != OMC_OK) return OMC_ERR_NOMEM;
   if (e->wf_counters.ensure(sizeof(WfCounters)) != OMC_OK) return OMC_ERR_NOMEM;
   char *qb = static_cast<char *>(S.queue.p);
@@ -1019,10 +1040,14 @@ omc_status run_wavefront(omc_engine *e, PrecisionState<R> &S, const omc_run_conf
       W.el_f[q - 2] = f;
       W.el_k[q - 2] = k;
       W.el_s[q - 2] = tag;
-    } else {
+    } else if (q < 6) {
       W.ei_f[q - 4] = f;
       W.ei_k[q - 4] = k;
       W.ei_s[q - 4] = tag;
+    } else {
+      W.pi_f[q - 6] = f;
+      W.pi_k[q - 6] = k;
+      W.pi_s[q - 6] = tag;
     }
   }
   WfCounters *wc = static_cast<WfCounters *>(e->wf_counters.p);

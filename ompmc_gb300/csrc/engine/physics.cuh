@@ -69,6 +69,10 @@ struct EmitTargets {
   int *ei_k;
   unsigned *ei_n;
   int *ei_s;
+  R *pi_f;            // photons waiting for their interaction
+  int *pi_k;
+  unsigned *pi_n;
+  int *pi_s;
 };
 
 __device__ __forceinline__ unsigned lanemask_lt() {
@@ -89,7 +93,7 @@ struct Lane {
   int np;    // top slot, -1 = empty (per-lane schedule)
   Particle<R> p;
   bool alive;           // wavefront: p still needs to be queued
-  bool defer_interactions = false;  // wavefront: queue discrete electron interactions
+  bool defer_interactions = false;  // wavefront: queue photon and discrete electron interactions
   bool pending_interaction = false; // wavefront: p ended its step at an interaction
   EmitTargets<R> out;   // wavefront: where this phase appends
   unsigned queue_cap;
@@ -239,6 +243,13 @@ struct Lane {
   }
   // The current electron, which ended its step at a discrete interaction.
   __device__ __forceinline__ void emit_pending() { emit_to(out.ei_f, out.ei_k, out.ei_n, p, out.ei_s); }
+  // A photon at its interaction point.  Its key holds iq + 1 = 1 for a
+  // split whose scattered photon is dropped and 3 for the surviving one.
+  __device__ __forceinline__ void emit_photon_interaction(const Particle<R> &q, bool survivor) {
+    Particle<R> t = q;
+    t.iq = survivor ? 2 : 0;
+    emit_to(out.pi_f, out.pi_k, out.pi_n, t, out.pi_s);
+  }
   __device__ __forceinline__ void take(const R *f, const int *k, unsigned slot, const int *tag) {
     if (tag) set_tag(__ldcg(tag + slot));
     size_t c = queue_cap;
