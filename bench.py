@@ -466,7 +466,9 @@ def run_ct_leg(args, local_rank):
 SERVE_WORKLOAD = ("dose-server mix: Poisson arrivals; phantom homogeneous water / z-slab / seeded blob at 64^3, "
                   "128^3 or 256x256x160 (2-4.7 mm voxels over a 30-48 cm box); source 1.25 MeV, synthetic 6 MV or "
                   "synthetic 250 kVp, 10x10 cm2 field at SSD 100 cm; histories log-uniform over [1e5, 1e8]; "
-                  "10 batches per job")
+                  "10 batches per job.  A fraction of the jobs are beamlet (dij) jobs instead: 50-500 bixels "
+                  "(0.5 cm) drawn from 1-3 beams of 10x10 cm2 at SAD 100 cm about the phantom centre, synthetic "
+                  "6 MV, the job's histories split evenly over its beamlets, relative threshold 1e-4, FP32 values")
 
 
 def serve_library():
@@ -514,7 +516,18 @@ def run_serve_leg(args, local_rank):
             isrc = int(rng.integers(3))
             nh = int(10 ** rng.uniform(5.0, np.log10(args.serve_max_histories)))
             nh -= nh % 10
-            draws.append((ip, isrc, max(nh, 10)))
+            bl = None
+            if rng.uniform() < args.serve_beamlet_frac:
+                isrc = 1
+                p = lib[ip][1]
+                iso = (0.5 * (p.xb[0] + p.xb[-1]), 0.5 * (p.yb[0] + p.yb[-1]), 0.5 * (p.zb[0] + p.zb[-1]))
+                angles = tuple(float(a) for a in rng.choice([0.0, 40.0, 80.0, 280.0, 320.0],
+                                                             size=int(rng.integers(1, 4)), replace=False))
+                full = W.beamlets(gantry_deg=angles, iso=iso, sad=100.0, bixel=0.5, field=10.0)
+                pick = np.sort(rng.choice(full.n, size=min(full.n, int(rng.integers(50, 501))), replace=False))
+                bl = W.Beamlets(full.ibeam[pick], full.source, full.corner[pick], full.side1[pick], full.side2[pick])
+                nh = max(nh - nh % (10 * bl.n), 10 * bl.n)
+            draws.append((ip, isrc, max(nh, 10), bl))
             if (ip, isrc) not in sources:
                 sources[(ip, isrc)] = api.build_source(inputs[isrc], phs[ip])
         mean_h = float(np.mean([d[2] for d in draws]))
@@ -531,16 +544,22 @@ def run_serve_leg(args, local_rank):
                                 1000, 10))
             ids = []
             t0 = time.perf_counter()
-            for (ip, isrc, nh), gap in zip(draws, gaps):
+            for (ip, isrc, nh, bl), gap in zip(draws, gaps):
                 time.sleep(gap)
-                ids.append(srv.submit(phs[ip], sources[(ip, isrc)], 0.7, 0.01, nh // 10, 10))
-            res = [srv.wait(i)[2] for i in ids]
+                if bl is None:
+                    ids.append(srv.submit(phs[ip], sources[(ip, isrc)], 0.7, 0.01, nh // 10, 10))
+                else:
+                    ids.append(srv.submit_dij(phs[ip], sources[(ip, isrc)], 0.7, 0.01, bl, nh // (10 * bl.n), 10,
+                                              rel_threshold=1e-4, fp32_values=True))
+            res = [(srv.wait(i) if d[3] is None else srv.wait_dij(i))[-1] for i, d in zip(ids, draws)]
             makespan = time.perf_counter() - t0
             st = srv.stats()
             srv.close()
             lat = np.array([r.finish_s - r.submit_s for r in res])
+            is_dij = np.array([d[3] is not None for d in draws])
             tot = sum(d[2] for d in draws)
             out[mode] = {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+                         "beamlet_jobs_p50_s": float(np.percentile(lat[is_dij], 50)) if is_dij.any() else None,
                          "mean_s": float(lat.mean()), "histories_per_s": tot / makespan,
                          "gpu_transport_s": st.transport_s, "rounds": int(st.rounds),
                          "max_resident": int(st.max_resident), "max_round_jobs": int(st.max_round_jobs)}
@@ -550,6 +569,7 @@ def run_serve_leg(args, local_rank):
         return {"metric": "job latency p50/p99 (s) and histories/s", "n_gpus": 1, "data": "synthetic",
                 "dtype": "f32", "config": {"workload": SERVE_WORKLOAD, "jobs": njobs, "rate_per_s": args.serve_rate,
                                            "mean_histories": mean_h, "total_histories": total,
+                                           "beamlet_jobs": int(sum(d[3] is not None for d in draws)),
                                            "seed": args.serve_seed},
                 "continuous": out["continuous"], "continuous_equal_shares": out["continuous_equal_shares"],
                 "one_at_a_time": out["one_at_a_time"]}
@@ -578,6 +598,7 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=0.5, help="job arrivals per second")
     ap.add_argument("--serve-max-histories", type=float, default=1e8)
     ap.add_argument("--serve-seed", type=int, default=5)
+    ap.add_argument("--serve-beamlet-frac", type=float, default=0.25, help="share of beamlet (dij) jobs in the mix")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

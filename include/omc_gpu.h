@@ -553,6 +553,26 @@ omc_status omc_server_wait(omc_server *s, long long id, double timeout_s,
                            double *accum_endep, double *accum_endep2,
                            omc_server_result *res);
 
+/* A beamlet job: the dose-influence matrix of bl on job's phantom, as
+ * omc_engine_run_dij computes it (job->source gives the spectrum and
+ * charge; its geometry is the beamlets').  nhist[i] histories for beamlet
+ * i, or job->nperbatch * job->nbatch each when nhist is NULL; job->nbatch
+ * batches.  All inputs are copied.  The job runs whole, in a turn of its
+ * own between rounds: when shortest-remaining-first picks it, or with
+ * equal shares when it is the oldest resident job.  Its RANMAR streams are
+ * the server's, advanced by ((id mod 512) + 1) * 2^20 streams; field
+ * rounds after it take streams from (513 + e mod 400) * 2^20 on, for the
+ * e-th such reseeding. */
+omc_status omc_server_submit_dij(omc_server *s, const omc_server_job *job,
+                                 const omc_beamlets *bl,
+                                 const long long *nhist, double rel_threshold,
+                                 int fp32_values, long long *id);
+
+/* Waits for beamlet job id as omc_server_wait does and hands over its dij
+ * (*out, freed with omc_dij_free); res->histories = all its histories. */
+omc_status omc_server_wait_dij(omc_server *s, long long id, double timeout_s,
+                               omc_dij **out, omc_server_result *res);
+
 typedef struct omc_server_stats {
     long long submitted, finished, rounds, histories;
     int max_resident;           /* most jobs resident at once              */

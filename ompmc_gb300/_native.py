@@ -188,6 +188,9 @@ def lib(path: str | None = None):
         "omc_server_submit": ([vp, pp(ServerJob_t), pp(C.c_longlong)], C.c_int),
         "omc_server_wait": ([vp, C.c_longlong, C.c_double, pp(C.c_double), pp(C.c_double), pp(ServerResult_t)],
                             C.c_int),
+        "omc_server_submit_dij": ([vp, pp(ServerJob_t), pp(Beamlets_t), pp(C.c_longlong), C.c_double, C.c_int,
+                                   pp(C.c_longlong)], C.c_int),
+        "omc_server_wait_dij": ([vp, C.c_longlong, C.c_double, pp(pp(Dij_t)), pp(ServerResult_t)], C.c_int),
         "omc_server_get_stats": ([vp, pp(ServerStats_t)], C.c_int),
         "omc_server_destroy": ([vp], None),
         "omc_engine_tune": ([vp, pp(RunConfig_t), C.c_longlong, pp(RunConfig_t), pp(C.c_double)], C.c_int),

@@ -308,7 +308,8 @@ class Server:
         names = (C.c_char_p * len(media))(*[m.encode() for m in media])
         self._h = C.c_void_p()
         check(N.lib().omc_server_create(C.byref(cfg), self._inp._h, len(media), names, C.byref(self._h)))
-        self._nreg = {}
+        self._nreg = {}  # field jobs: regions
+        self._dij = {}  # beamlet jobs: FP32 values
 
     def submit(self, phantom, source, ecut, pcut, nperbatch, nbatch):
         """phantom: :class:`Phantom`; source: a POINTER(Source_t) (e.g.
@@ -325,13 +326,41 @@ class Server:
                            prob.nperbatch if nperbatch is None else nperbatch,
                            prob.nbatch if nbatch is None else nbatch)
 
+    def submit_dij(self, phantom, source, ecut, pcut, beamlets, nperbatch, nbatch, nhist=None, rel_threshold=1e-4,
+                   fp32_values=False):
+        """A beamlet job (omc_server_submit_dij): the dose-influence matrix of
+        `beamlets` (:class:`ompmc_gb300.workloads.Beamlets`) on `phantom`,
+        nhist[i] histories for beamlet i (default nperbatch * nbatch each).
+        Returns the job id; collect it with :meth:`wait_dij`."""
+        job = N.ServerJob_t(phantom._p, source, float(ecut), float(pcut), int(nperbatch), int(nbatch))
+        bl, keep = _beamlets_t(beamlets)
+        nh = None if nhist is None else np.ascontiguousarray(nhist, dtype=np.int64)
+        jid = C.c_longlong()
+        check(N.lib().omc_server_submit_dij(self._h, C.byref(job), C.byref(bl),
+                                            None if nh is None else nh.ctypes.data_as(C.POINTER(C.c_longlong)),
+                                            float(rel_threshold), 1 if fp32_values else 0, C.byref(jid)))
+        del keep
+        self._dij[jid.value] = bool(fp32_values)
+        return jid.value
+
+    def wait_dij(self, jid, timeout=-1.0):
+        """(col_ptr, row_idx, values, ServerResult_t) of a beamlet job."""
+        fp32 = self._dij.get(jid, False)
+        out = C.POINTER(N.Dij_t)()
+        r = N.ServerResult_t()
+        check(N.lib().omc_server_wait_dij(self._h, jid, float(timeout), C.byref(out), C.byref(r)))
+        del self._dij[jid]
+        return (*_take_dij(out, fp32), r)
+
     def wait(self, jid, timeout=-1.0):
         """(accum_endep, accum_endep2, ServerResult_t) of a finished job."""
-        nreg = self._nreg.pop(jid)
+        nreg = self._nreg.get(jid, 0)  # 0: not a field job of this wrapper; the library says why
         a = np.zeros(nreg)
         a2 = np.zeros(nreg)
         r = N.ServerResult_t()
-        check(N.lib().omc_server_wait(self._h, jid, float(timeout), _dptr(a), _dptr(a2), C.byref(r)))
+        check(N.lib().omc_server_wait(self._h, jid, float(timeout), _dptr(a) if nreg else None,
+                                      _dptr(a2) if nreg else None, C.byref(r)))
+        del self._nreg[jid]
         return a, a2, r
 
     def stats(self):

@@ -52,6 +52,20 @@ struct Job {
   double submit_s = 0, admit_s = 0, finish_s = 0;
   int rounds = 0;
   omc_status status = OMC_OK;
+  // beamlet (dij) jobs: run whole, in a turn of their own
+  bool dij = false;
+  int nbeams = 0;
+  std::vector<int> ibeam;
+  std::vector<double> bl[12];  // x/y/z source (nbeams), corner, side1, side2 (nbeamlets)
+  std::vector<long long> nhist;
+  double rel_threshold = 0;
+  int fp32_values = 0;
+  omc_dij *dij_out = nullptr;
+  long long total() const {
+    long long t = 0;
+    for (long long h : nhist) t += h;
+    return t;
+  }
 };
 
 }  // namespace
@@ -78,26 +92,75 @@ struct omc_server {
 
 namespace {
 
-// Regions of a job against the server's tables: the phantom with its media
-// renumbered onto the server's, then initRegions (omc_regions_build).
-omc_status upload_job(omc_server *s, Job &j) {
+// A job's phantom with its media renumbered onto the server's, and its
+// regions against the server's tables (initRegions, omc_regions_build).
+struct JobGeometry {
+  omc_phantom *ph = nullptr;
+  omc_input *in = nullptr;
+  omc_regions *reg = nullptr;
+  ~JobGeometry() {
+    omc_regions_free(reg);
+    omc_input_free(in);
+    omc_phantom_free(ph);
+  }
+};
+
+omc_status job_geometry(omc_server *s, const Job &j, JobGeometry &g) {
   omc_status st;
   std::vector<const char *> names;
   for (const auto &m : s->media) names.push_back(m.c_str());
-  omc_phantom *ph = nullptr;
   if ((st = omc_phantom_create(static_cast<int>(names.size()), names.data(), j.ph.nx, j.ph.ny, j.ph.nz,
                                j.ph.xb.data(), j.ph.yb.data(), j.ph.zb.data(), j.ph.med.data(), j.ph.density.data(),
-                               &ph)) != OMC_OK)
+                               &g.ph)) != OMC_OK)
     return st;
   char text[256];
   std::snprintf(text, sizeof text, "global ecut = %.17g\nglobal pcut = %.17g\n", j.ecut, j.pcut);
-  omc_input *in = nullptr;
-  omc_regions *reg = nullptr;
-  if ((st = omc_input_from_string(text, &in)) == OMC_OK && (st = omc_regions_build(in, ph, s->tab, &reg)) == OMC_OK)
-    st = omc_engine_job_add(s->eng, ph, reg, &j.src, j.nperbatch, j.nbatch, s->cfg.precision, &j.dev);
-  omc_regions_free(reg);
-  omc_input_free(in);
-  omc_phantom_free(ph);
+  if ((st = omc_input_from_string(text, &g.in)) != OMC_OK) return st;
+  return omc_regions_build(g.in, g.ph, s->tab, &g.reg);
+}
+
+// Field jobs go onto the device at admission; beamlet jobs stay on the
+// host until their turn.
+omc_status upload_job(omc_server *s, Job &j) {
+  if (j.dij) return OMC_OK;
+  JobGeometry g;
+  omc_status st = job_geometry(s, j, g);
+  if (st != OMC_OK) return st;
+  return omc_engine_job_add(s->eng, g.ph, g.reg, &j.src, j.nperbatch, j.nbatch, s->cfg.precision, &j.dev);
+}
+
+// A beamlet job, whole, on the server's tables (omc_engine_run_dij).  Its
+// RANMAR streams start far from the server's own and from every other
+// beamlet job's.
+omc_status run_dij_job(omc_server *s, Job &j) {
+  JobGeometry g;
+  omc_status st = job_geometry(s, j, g);
+  if (st != OMC_OK) return st;
+  if ((st = omc_engine_set_geometry(s->eng, g.ph, g.reg)) != OMC_OK) return st;
+  if ((st = omc_engine_set_source(s->eng, &j.src)) != OMC_OK) return st;
+  omc_beamlets b{static_cast<int>(j.ibeam.size()), j.nbeams, j.ibeam.data(), j.bl[0].data(), j.bl[1].data(),
+                 j.bl[2].data(), j.bl[3].data(), j.bl[4].data(), j.bl[5].data(), j.bl[6].data(), j.bl[7].data(),
+                 j.bl[8].data(), j.bl[9].data(), j.bl[10].data(), j.bl[11].data()};
+  if ((st = omc_engine_set_beamlets(s->eng, &b)) != OMC_OK) return st;
+  omc_run_config rc;
+  std::memset(&rc, 0, sizeof rc);
+  rc.nperbatch = 1;
+  rc.nbatch = j.nbatch;
+  omc_stream_seeds(s->cfg.ixx, s->cfg.jxx, (j.id % 512 + 1) << 20, &rc.ixx, &rc.jxx);
+  rc.nsplit = s->cfg.nsplit;
+  rc.precision = s->cfg.precision;
+  omc_dij_config dc;
+  std::memset(&dc, 0, sizeof dc);
+  dc.rel_threshold = j.rel_threshold;
+  dc.nhist = j.nhist.data();
+  dc.fp32_values = j.fp32_values;
+  omc_run_stats rs{};
+  st = omc_engine_run_dij(s->eng, &rc, &dc, &j.dij_out, &rs);
+  if (st == OMC_OK) {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->st.histories += rs.histories;
+    s->st.transport_s += rs.transport_ms * 1e-3;
+  }
   return st;
 }
 
@@ -137,13 +200,56 @@ void admission_loop(omc_server *s) {
 }
 
 void scheduler_loop(omc_server *s) {
+  // Field rounds continue their streams from round to round.  After a
+  // beamlet turn (which seeds the engine's streams with its own) they are
+  // seeded again, epoch e at stream (512 + e) * 2^20 of the server's
+  // sequence, so no number is drawn twice.
   bool seeded = false;
+  long long epoch = 0;
   std::unique_lock<std::mutex> lk(s->mu);
   for (;;) {
     s->cv_sched.wait(lk, [&] { return s->stop || !s->resident.empty(); });
     if (s->stop) return;
-    std::vector<std::shared_ptr<Job>> round = s->resident;
+    std::vector<std::shared_ptr<Job>> all = s->resident;
     lk.unlock();
+    // A beamlet job runs whole in a turn of its own: when it has the fewest
+    // histories left (shortest remaining first) or, with equal shares, when
+    // it is the oldest resident job.
+    std::shared_ptr<Job> turn;
+    {
+      long long best = -1;
+      for (auto &j : all) {
+        long long left = j->dij ? j->total() : omc_job_histories(j->dev) - omc_job_done(j->dev);
+        if (best < 0 || left < best) {
+          best = left;
+          turn = j;
+        }
+      }
+      if (s->cfg.policy == OMC_SERVE_EQUAL_SHARES) turn = all.front();
+      if (!turn->dij) turn = nullptr;
+    }
+    if (turn) {
+      omc_status st = run_dij_job(s, *turn);
+      lk.lock();
+      turn->rounds = 1;
+      turn->status = st;
+      turn->finish_s = s->now();
+      turn->state = st == OMC_OK ? JobState::Done : JobState::Failed;
+      s->resident.erase(std::remove(s->resident.begin(), s->resident.end(), turn), s->resident.end());
+      s->resident_bytes -= static_cast<long long>(turn->bytes);
+      s->st.finished++;
+      s->st.rounds++;
+      s->cv_done.notify_all();
+      s->cv_admit.notify_all();
+      if (seeded) {
+        seeded = false;
+        epoch++;
+      }
+      continue;
+    }
+    std::vector<std::shared_ptr<Job>> round;
+    for (auto &j : all)
+      if (!j->dij) round.push_back(j);
     const long long R = s->cfg.round_histories;
     std::vector<long long> left(round.size()), quota(round.size(), 0);
     for (size_t i = 0; i < round.size(); i++) left[i] = omc_job_histories(round[i]->dev) - omc_job_done(round[i]->dev);
@@ -194,6 +300,7 @@ void scheduler_loop(omc_server *s) {
       rc.nbatch = 1;
       rc.ixx = s->cfg.ixx;
       rc.jxx = s->cfg.jxx;
+      if (epoch) omc_stream_seeds(s->cfg.ixx, s->cfg.jxx, (512 + (epoch - 1) % 400 + 1) << 20, &rc.ixx, &rc.jxx);
       rc.nsplit = s->cfg.nsplit;
       rc.precision = s->cfg.precision;
       rc.continue_streams = seeded ? 1 : 0;
@@ -281,9 +388,10 @@ extern "C" omc_status omc_server_create(const omc_server_config *cfg, const omc_
   return OMC_OK;
 }
 
-extern "C" omc_status omc_server_submit(omc_server *s, const omc_server_job *job, long long *id) {
-  if (!s || !job || !job->phantom || !job->source || !id) return fail(OMC_ERR_ARG, "null argument");
-  if (job->nbatch < 1 || job->nperbatch < 1) return fail(OMC_ERR_ARG, "need nbatch >= 1 and nperbatch >= 1");
+namespace {
+
+// Host copy of a job, its media renumbered onto the server's by name.
+omc_status copy_job(omc_server *s, const omc_server_job *job, std::shared_ptr<Job> &out) {
   const omc_phantom *p = job->phantom;
   auto j = std::make_shared<Job>();
   j->ph.nx = p->nx;
@@ -312,7 +420,11 @@ extern "C" omc_status omc_server_submit(omc_server *s, const omc_server_job *job
   j->pcut = job->pcut;
   j->nperbatch = job->nperbatch;
   j->nbatch = job->nbatch;
-  j->bytes = omc_job_device_bytes(p, job->nbatch, s->cfg.precision);
+  out = j;
+  return OMC_OK;
+}
+
+void enqueue(omc_server *s, const std::shared_ptr<Job> &j, long long *id) {
   std::lock_guard<std::mutex> lk(s->mu);
   j->id = s->next_id++;
   j->submit_s = s->now();
@@ -321,6 +433,85 @@ extern "C" omc_status omc_server_submit(omc_server *s, const omc_server_job *job
   s->st.submitted++;
   *id = j->id;
   s->cv_admit.notify_all();
+}
+
+}  // namespace
+
+extern "C" omc_status omc_server_submit(omc_server *s, const omc_server_job *job, long long *id) {
+  if (!s || !job || !job->phantom || !job->source || !id) return fail(OMC_ERR_ARG, "null argument");
+  if (job->nbatch < 1 || job->nperbatch < 1) return fail(OMC_ERR_ARG, "need nbatch >= 1 and nperbatch >= 1");
+  std::shared_ptr<Job> j;
+  omc_status st = copy_job(s, job, j);
+  if (st != OMC_OK) return st;
+  j->bytes = omc_job_device_bytes(job->phantom, job->nbatch, s->cfg.precision);
+  enqueue(s, j, id);
+  return OMC_OK;
+}
+
+extern "C" omc_status omc_server_submit_dij(omc_server *s, const omc_server_job *job, const omc_beamlets *bl,
+                                            const long long *nhist, double rel_threshold, int fp32_values,
+                                            long long *id) {
+  if (!s || !job || !job->phantom || !job->source || !bl || !id) return fail(OMC_ERR_ARG, "null argument");
+  if (job->nbatch < 1) return fail(OMC_ERR_ARG, "need nbatch >= 1");
+  if (bl->nbeamlets < 1 || bl->nbeams < 1) return fail(OMC_ERR_ARG, "need at least one beamlet and one beam");
+  if (!(rel_threshold >= 0.0)) return fail(OMC_ERR_ARG, "relative dose threshold must be >= 0");
+  for (int i = 0; i < bl->nbeamlets; i++)
+    if (bl->ibeam[i] < 0 || bl->ibeam[i] >= bl->nbeams) return fail(OMC_ERR_ARG, "beamlet %d: bad beam", i);
+  if (nhist)
+    for (int i = 0; i < bl->nbeamlets; i++)
+      if (nhist[i] < 1) return fail(OMC_ERR_ARG, "beamlet %d: need at least one history", i);
+  if (!nhist && job->nperbatch < 1) return fail(OMC_ERR_ARG, "need nperbatch >= 1");
+  std::shared_ptr<Job> j;
+  omc_status st = copy_job(s, job, j);
+  if (st != OMC_OK) return st;
+  j->dij = true;
+  j->nbeams = bl->nbeams;
+  j->ibeam.assign(bl->ibeam, bl->ibeam + bl->nbeamlets);
+  const double *src[12] = {bl->xsource, bl->ysource, bl->zsource, bl->xcorner, bl->ycorner, bl->zcorner,
+                           bl->xside1,  bl->yside1,  bl->zside1,  bl->xside2,  bl->yside2,  bl->zside2};
+  for (int k = 0; k < 12; k++) j->bl[k].assign(src[k], src[k] + (k < 3 ? bl->nbeams : bl->nbeamlets));
+  j->nhist.resize(bl->nbeamlets);
+  for (int i = 0; i < bl->nbeamlets; i++)
+    j->nhist[i] = nhist ? nhist[i] : job->nperbatch * static_cast<long long>(job->nbatch);
+  j->rel_threshold = rel_threshold;
+  j->fp32_values = fp32_values;
+  // Device footprint while it runs: the beamlet tallies (bounded by the
+  // budget, which omc_engine_run_dij splits into groups) and the phantom.
+  size_t nreg = static_cast<size_t>(job->phantom->nx) * job->phantom->ny * job->phantom->nz + 1;
+  size_t tally = static_cast<size_t>(bl->nbeamlets) * nreg * sizeof(double);
+  j->bytes = std::min<size_t>(tally, static_cast<size_t>(s->cfg.hbm_budget)) + nreg * 24;
+  enqueue(s, j, id);
+  return OMC_OK;
+}
+
+extern "C" omc_status omc_server_wait_dij(omc_server *s, long long id, double timeout_s, omc_dij **out,
+                                         omc_server_result *res) {
+  if (!s || !out) return fail(OMC_ERR_ARG, "null argument");
+  *out = nullptr;
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto it = s->jobs.find(id);
+  if (it == s->jobs.end()) return fail(OMC_ERR_ARG, "unknown job %lld", id);
+  std::shared_ptr<Job> j = it->second;
+  if (!j->dij) return fail(OMC_ERR_ARG, "job %lld is not a beamlet job", id);
+  auto done = [&] { return j->state == JobState::Done || j->state == JobState::Failed; };
+  if (timeout_s < 0) {
+    s->cv_done.wait(lk, done);
+  } else if (!s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), done)) {
+    return fail(OMC_ERR_LIMIT, "job %lld not finished after %.3f s", id, timeout_s);
+  }
+  s->jobs.erase(it);
+  if (res) {
+    res->ensrc = 0;
+    res->histories = j->total();
+    res->submit_s = j->submit_s;
+    res->admit_s = j->admit_s;
+    res->finish_s = j->finish_s;
+    res->rounds = j->rounds;
+    res->status = j->status;
+  }
+  if (j->state == JobState::Failed) return fail(j->status, "job %lld failed", id);
+  *out = j->dij_out;
+  j->dij_out = nullptr;
   return OMC_OK;
 }
 
@@ -331,6 +522,7 @@ extern "C" omc_status omc_server_wait(omc_server *s, long long id, double timeou
   auto it = s->jobs.find(id);
   if (it == s->jobs.end()) return fail(OMC_ERR_ARG, "unknown job %lld", id);
   std::shared_ptr<Job> j = it->second;
+  if (j->dij) return fail(OMC_ERR_ARG, "job %lld is a beamlet job: use omc_server_wait_dij", id);
   auto done = [&] { return j->state == JobState::Done || j->state == JobState::Failed; };
   if (timeout_s < 0) {
     s->cv_done.wait(lk, done);
@@ -373,6 +565,8 @@ extern "C" void omc_server_destroy(omc_server *s) {
   for (auto &j : s->resident)
     if (j->dev) omc_engine_job_remove(s->eng, j->dev);
   s->resident.clear();
+  for (auto &kv : s->jobs)
+    if (kv.second->dij_out) omc_dij_free(kv.second->dij_out);
   omc_engine_destroy(s->eng);
   omc_tables_free(s->tab);
   delete s;

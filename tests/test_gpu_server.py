@@ -2,9 +2,12 @@
 ABI: a job advanced in rounds of uneven size gives the batch sums
 omc_engine_run gives; a job gives the same result alone and in a mix of
 jobs with other phantoms, sources and particle kinds; admission respects
-the device-memory budget; small jobs overtake large ones."""
+the device-memory budget; small jobs overtake large ones; beamlet (dij)
+jobs queued among field jobs give the dij omc_engine_run_dij gives."""
 
 import ctypes as C
+import dataclasses
+import time
 
 import numpy as np
 import pytest
@@ -136,5 +139,82 @@ def test_unknown_medium_is_refused(native, tmp_path):
         with pytest.raises(N.OmcError) as e:
             srv.submit(phantom, C.pointer(src), 0.7, 0.01, 10, 2)
         assert e.value.status == 4
+    finally:
+        srv.close()
+
+
+def column_sums(col, vals):
+    return np.array([vals[col[j]:col[j + 1]].sum() for j in range(len(col) - 1)])
+
+
+def test_beamlet_jobs_beside_field_jobs(engine, problem_factory, tmp_path):
+    """Beamlet jobs queued among a field job: each gives the dij that
+    omc_engine_run_dij gives (per-beamlet integral doses over 6 jobs against
+    6 engine runs, within their spread), and the field job, whose rounds
+    are cut by the beamlet turns, gives the dose omc_engine_run gives."""
+    from cases import dij_case
+
+    inp, _, bl, _, _, _ = dij_case("dij_slab", str(tmp_path / "d"), ncase=1000, nbatch=2)
+    prob = api.Problem.from_file(inp)
+    field = problem_factory("slab_6mv", ncase=2000000, nbatch=10, seeds=(3, 4))
+    g = lambda key: float(prob.input.get(key))
+    k = 6
+    srv = api.Server(MEDIA, data_text(), precision=api.FP32, round_histories=100000)
+    try:
+        fid = srv.submit_problem(field)
+        t0 = time.perf_counter()
+        while srv.stats().rounds < 1 and time.perf_counter() - t0 < 60:
+            time.sleep(0.001)
+        ids = [srv.submit_dij(prob.phantom, prob.source, g("global ecut"), g("global pcut"), bl, 1000, 2,
+                              rel_threshold=0.0) for _ in range(k)]
+        with pytest.raises(N.OmcError):
+            srv.wait(ids[0])  # a beamlet job is collected with wait_dij
+        outs = [srv.wait_dij(i) for i in ids]
+        fa, fa2, fr = srv.wait(fid)
+        st = srv.stats()
+    finally:
+        srv.close()
+    for col, rows, vals, r in outs:
+        assert r.status == 0 and r.rounds == 1
+        assert r.histories == bl.n * 2000
+        assert len(col) == bl.n + 1 and col[-1] == len(rows) == len(vals)
+    assert fr.rounds > 10 and st.finished == k + 1
+    assert fr.finish_s > max(o[3].finish_s for o in outs)  # beamlet turns came between its rounds
+    srv_sums = np.stack([column_sums(o[0], o[2]) for o in outs])
+    engine.load(prob)
+    engine.set_beamlets(bl)
+    eng_sums = []
+    for i in range(k):
+        col, rows, vals, est = engine.run_dij(rel_threshold=0.0, precision=api.FP32, seeds=(61 + i, 5))
+        eng_sums.append(column_sums(col, vals))
+    eng_sums = np.stack(eng_sums)
+    z = (srv_sums.mean(0) - eng_sums.mean(0)) / np.sqrt(srv_sums.var(0, ddof=1) / k + eng_sums.var(0, ddof=1) / k)
+    assert np.mean(np.abs(z) < 3) > 0.9, z
+    assert abs(srv_sums.mean(0).sum() / eng_sums.mean(0).sum() - 1) < 0.02
+    # distinct beamlet jobs draw from distinct streams
+    assert not np.array_equal(outs[0][2], outs[1][2])
+    engine.load(field)
+    ref, ref2, _ = engine.run(precision=api.FP32, seeds=(29, 31))
+    same_distribution(fa, fa2, ref, ref2, field.nbatch, field.nperbatch * field.nbatch)
+
+
+def test_beamlet_job_errors(native, tmp_path):
+    from cases import dij_case
+
+    inp, _, bl, _, _, _ = dij_case("dij_slab", str(tmp_path / "d"))
+    prob = api.Problem.from_file(inp)
+    srv = api.Server(MEDIA, data_text(), precision=api.FP32)
+    try:
+        args = (prob.phantom, prob.source, 0.7, 0.01)
+        with pytest.raises(N.OmcError) as e:
+            srv.submit_dij(*args, bl, 10, 1, rel_threshold=-1.0)
+        assert e.value.status == 1
+        with pytest.raises(N.OmcError) as e:
+            srv.submit_dij(*args, bl, 10, 1, nhist=np.zeros(bl.n, np.int64))
+        assert e.value.status == 1
+        bad = dataclasses.replace(bl, ibeam=np.full(bl.n, 7, np.int32))
+        with pytest.raises(N.OmcError) as e:
+            srv.submit_dij(*args, bad, 10, 1)
+        assert e.value.status == 1
     finally:
         srv.close()
