@@ -511,20 +511,21 @@ def run_serve_leg(args, local_rank):
         sources = {}
         njobs = args.serve_jobs
         draws = []
+        brng = np.random.default_rng(args.serve_seed + 1000)  # beamlet choices apart: field draws stay as they were
         for _ in range(njobs):
             ip = int(rng.integers(len(phs)))
             isrc = int(rng.integers(3))
             nh = int(10 ** rng.uniform(5.0, np.log10(args.serve_max_histories)))
             nh -= nh % 10
             bl = None
-            if rng.uniform() < args.serve_beamlet_frac:
+            if brng.uniform() < args.serve_beamlet_frac:
                 isrc = 1
                 p = lib[ip][1]
                 iso = (0.5 * (p.xb[0] + p.xb[-1]), 0.5 * (p.yb[0] + p.yb[-1]), 0.5 * (p.zb[0] + p.zb[-1]))
-                angles = tuple(float(a) for a in rng.choice([0.0, 40.0, 80.0, 280.0, 320.0],
-                                                             size=int(rng.integers(1, 4)), replace=False))
+                angles = tuple(float(a) for a in brng.choice([0.0, 40.0, 80.0, 280.0, 320.0],
+                                                              size=int(brng.integers(1, 4)), replace=False))
                 full = W.beamlets(gantry_deg=angles, iso=iso, sad=100.0, bixel=0.5, field=10.0)
-                pick = np.sort(rng.choice(full.n, size=min(full.n, int(rng.integers(50, 501))), replace=False))
+                pick = np.sort(brng.choice(full.n, size=min(full.n, int(brng.integers(50, 501))), replace=False))
                 bl = W.Beamlets(full.ibeam[pick], full.source, full.corner[pick], full.side1[pick], full.side2[pick])
                 nh = max(nh - nh % (10 * bl.n), 10 * bl.n)
             draws.append((ip, isrc, max(nh, 10), bl))
