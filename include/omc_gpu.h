@@ -372,6 +372,12 @@ omc_status omc_engine_trace_read(omc_engine *e, long long *out, int cap, int *n)
 /* Free and total device memory of a CUDA device (bytes). */
 omc_status omc_device_memory(int device, size_t *free_bytes, size_t *total_bytes);
 
+/* Throughput of scattered FP64 atomicAdd into an array of nreg doubles
+ * (atomics/s; ausgab's pattern: every lane of a warp adds to its own
+ * voxel), best of 3 launches of 8 blocks x 256 threads per SM, 1024 adds
+ * per thread.  The denominator of the transport kernels' tally rate. */
+omc_status omc_measure_atomic_rate(int device, long long nreg, double *per_s);
+
 /* RANMAR streams on the device (bit-exact with initRandom/setRandom,
  * omc_random.c:58-187).  Stream k is seeded with the k-th pair of the
  * sequence (ixx, jxx), (ixx, jxx+1), ..., (the reference's per-thread

@@ -197,6 +197,7 @@ def lib(path: str | None = None):
         "omc_engine_trace": ([vp, C.c_int], C.c_int),
         "omc_engine_trace_read": ([vp, pp(C.c_longlong), C.c_int, pp(C.c_int)], C.c_int),
         "omc_device_memory": ([C.c_int, pp(C.c_size_t), pp(C.c_size_t)], C.c_int),
+        "omc_measure_atomic_rate": ([C.c_int, C.c_longlong, pp(C.c_double)], C.c_int),
         "omc_gpu_ranmar": ([C.c_int, C.c_int, C.c_int, C.c_int, C.c_longlong, pp(C.c_int32)], C.c_int),
         "omc_stream_seeds": ([C.c_int, C.c_int, C.c_longlong, pp(C.c_int), pp(C.c_int)], None),
     }

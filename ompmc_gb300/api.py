@@ -435,6 +435,14 @@ def gpu_ranmar(ixx, jxx, nstreams, n, device=0):
     return out
 
 
+def atomic_rate(nreg, device=0):
+    """Scattered FP64 atomicAdd throughput over nreg doubles (atomics/s,
+    omc_measure_atomic_rate)."""
+    r = C.c_double()
+    check(N.lib().omc_measure_atomic_rate(device, int(nreg), C.byref(r)))
+    return r.value
+
+
 def stream_seeds(ixx, jxx, k):
     a, b = C.c_int(), C.c_int()
     N.lib().omc_stream_seeds(ixx, jxx, k, C.byref(a), C.byref(b))

@@ -1855,6 +1855,59 @@ extern "C" omc_status omc_device_memory(int device, size_t *free_bytes, size_t *
   return OMC_OK;
 }
 
+namespace {
+
+// Scattered FP64 atomicAdd, the access pattern of ausgab in the wavefront
+// schedule: the 32 lanes of a warp hold unrelated particles, so each adds
+// to its own voxel.  Indices come from a per-thread xorshift32 sequence,
+// mapped onto [0, nreg) by a 32x64-bit multiply-high.
+__global__ void atomic_rate_kernel(double *t, unsigned long long nreg, int per_thread, unsigned seed) {
+  unsigned long long tid = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
+  unsigned h = (static_cast<unsigned>(tid) * 0x9E3779B9u ^ seed) | 1u;
+  for (int k = 0; k < per_thread; k++) {
+    h ^= h << 13;
+    h ^= h >> 17;
+    h ^= h << 5;
+    atomicAdd(t + ((static_cast<unsigned long long>(h) * nreg) >> 32), 1.0);
+  }
+}
+
+}  // namespace
+
+extern "C" omc_status omc_measure_atomic_rate(int device, long long nreg, double *per_s) {
+  if (!per_s || nreg < 1 || nreg > (1ll << 32)) return fail(OMC_ERR_ARG, "need 1 <= nreg <= 2^32");
+  *per_s = 0;
+  CUDA_TRY(cudaSetDevice(device));
+  int sms = 0;
+  CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  DevBuf t;
+  omc_status st = t.ensure(static_cast<size_t>(nreg) * sizeof(double));
+  if (st != OMC_OK) return st;
+  const int threads = 256, per = 1024, blocks = sms * 8;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 0;
+  cudaError_t err = cudaMemset(t.p, 0, static_cast<size_t>(nreg) * sizeof(double));
+  for (int rep = 0; rep < 4 && err == cudaSuccess; rep++) {  // first launch warms up
+    cudaEventRecord(e0);
+    atomic_rate_kernel<<<blocks, threads>>>(static_cast<double *>(t.p), static_cast<unsigned long long>(nreg), per,
+                                            0x2545F491u + rep);
+    cudaEventRecord(e1);
+    err = cudaEventSynchronize(e1);
+    float ms = 0;
+    if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+    if (rep > 0 && (best == 0 || ms < best)) best = ms;
+  }
+  if (err == cudaSuccess) err = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  t.release();
+  if (err != cudaSuccess) return fail(OMC_ERR_CUDA, "atomic rate: %s", cudaGetErrorString(err));
+  *per_s = static_cast<double>(blocks) * threads * per / (best * 1e-3);
+  return OMC_OK;
+}
+
 extern "C" void omc_stream_seeds(int ixx, int jxx, long long k, int *ixx_k, int *jxx_k) {
   stream_seeds(ixx, jxx, k, ixx_k, jxx_k);
 }
