@@ -255,6 +255,12 @@ typedef struct omc_run_config {
     int chunk_events;    /* wavefront: condensed-history steps a thread
                             takes with one electron before it goes back to
                             the queue; 0 = auto                           */
+    int drain_per_warp;  /* wavefront: once every history is injected and
+                            fewer than this many particles per 32 threads
+                            are in flight (the end-of-run drain), electron
+                            interactions run inline and a take follows an
+                            electron to the end of its track; 0 = auto,
+                            -1 = never                                    */
 } omc_run_config;
 
 typedef enum omc_schedule {

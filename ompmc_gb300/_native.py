@@ -62,7 +62,8 @@ class RunConfig_t(C.Structure):
     _fields_ = [("nperbatch", C.c_longlong), ("nbatch", C.c_int), ("ixx", C.c_int), ("jxx", C.c_int),
                 ("nsplit", C.c_int), ("precision", C.c_int), ("nlanes", C.c_int),
                 ("stack_depth", C.c_int), ("serial", C.c_int), ("continue_streams", C.c_int),
-                ("schedule", C.c_int), ("inflight", C.c_longlong), ("chunk_events", C.c_int)]
+                ("schedule", C.c_int), ("inflight", C.c_longlong), ("chunk_events", C.c_int),
+                ("drain_per_warp", C.c_int)]
 
 
 class RunStats_t(C.Structure):

@@ -207,18 +207,19 @@ class Engine:
 
     @staticmethod
     def config(nperbatch, nbatch, seeds=(97, 33), nsplit=1, precision=FP64, nlanes=0, stack_depth=0, serial=0,
-               continue_streams=0, schedule=AUTO, inflight=0, chunk_events=0):
+               continue_streams=0, schedule=AUTO, inflight=0, chunk_events=0, drain_per_warp=0):
         return N.RunConfig_t(int(nperbatch), int(nbatch), int(seeds[0]), int(seeds[1]), int(nsplit),
                              int(precision), int(nlanes), int(stack_depth), int(serial), int(continue_streams),
-                             int(schedule), int(inflight), int(chunk_events))
+                             int(schedule), int(inflight), int(chunk_events), int(drain_per_warp))
 
     def run(self, nperbatch=None, nbatch=None, seeds=None, nsplit=None, precision=FP64, nlanes=0,
-            stack_depth=0, serial=0, continue_streams=0, schedule=AUTO, inflight=0, chunk_events=0):
+            stack_depth=0, serial=0, continue_streams=0, schedule=AUTO, inflight=0, chunk_events=0,
+            drain_per_warp=0):
         p = self._problem
         cfg = self.config(p.nperbatch if nperbatch is None else nperbatch, p.nbatch if nbatch is None else nbatch,
                           p.seeds if seeds is None else seeds, p.nsplit if nsplit is None else nsplit,
                           precision, nlanes, stack_depth, serial, continue_streams, schedule, inflight,
-                          chunk_events)
+                          chunk_events, drain_per_warp)
         a = np.zeros(p.nreg)
         a2 = np.zeros(p.nreg)
         st = N.RunStats_t()

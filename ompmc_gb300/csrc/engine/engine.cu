@@ -179,9 +179,22 @@ struct Wavefront {
   unsigned long long *trace;  // per iteration {ns, photons, electrons, injected}, or null
   int trace_cap;              // iterations the trace holds
   int chunk_events;           // electron steps per take before re-queueing
+  unsigned long long drain_below;  // drain mode below this many particles in flight
 };
 
 constexpr int kDefaultChunkEvents = 1;
+
+// End-of-run drain: once every history is injected and fewer than
+// kDrainPerWarp particles per 32 threads are in flight, the GPU is short
+// of work and each particle's remaining events would take one iteration
+// each.  Electron interactions then run inline and an electron take runs up
+// to kDrainSteps condensed-history steps, so a track ends in one iteration.
+// Above that the one-step takes keep warps full, which is worth more.
+// Measured on the 6 MV slab, 10 batches in one launch, job time against no
+// drain mode: 32 per warp FP32 3.4% and FP64 8.7% shorter; 8 per warp FP32
+// 2.0% shorter; 128 per warp FP32 0.7% shorter but FP64 12% longer.
+constexpr int kDrainPerWarp = 32;
+constexpr int kDrainSteps = 4096;
 
 template <typename R>
 constexpr unsigned long long kInflightPerThread = sizeof(R) == 4 ? 128 : 64;
@@ -262,6 +275,7 @@ __global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) wavefront_ke
       r[3] = injected;
     }
     if (remaining <= 0 && inflight == 0) break;
+    const bool drain = remaining <= 0 && inflight < W.drain_below;
     long long m = static_cast<long long>(W.target) - static_cast<long long>(inflight);
     if (m < 0) m = 0;
     if (m > remaining) m = remaining;
@@ -326,13 +340,19 @@ __global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) wavefront_ke
           // this electron; it goes back to a queue if it is still alive
           // (or if an interaction left a photon on top), to the
           // interaction queue if its step ended at a deferred interaction.
+          // In the drain the interaction runs at once and the take goes on
+          // with whatever electron is left on top.
           L.take(W.el_f[bin], W.el_k[bin], static_cast<unsigned>(k), W.el_s[bin]);
           L.pending_interaction = false;
           int n = 0;
           do {
             L.electron_event();
             events++;
-          } while (L.alive && !L.pending_interaction && L.p.iq != 0 && ++n < W.chunk_events);
+            if (drain && L.pending_interaction) {
+              L.pending_interaction = false;
+              L.deferred_interaction();
+            }
+          } while (L.alive && !L.pending_interaction && L.p.iq != 0 && ++n < (drain ? kDrainSteps : W.chunk_events));
           if (L.alive) {
             if (L.pending_interaction) L.emit_pending();
             else L.emit(L.p);
@@ -1064,6 +1084,11 @@ omc_status run_wavefront(omc_engine *e, PrecisionState<R> &S, const omc_run_conf
   W.trace = static_cast<unsigned long long *>(e->trace.p);
   W.trace_cap = e->trace_cap;
   W.chunk_events = cfg->chunk_events > 0 ? cfg->chunk_events : kDefaultChunkEvents;
+  W.drain_below = cfg->drain_per_warp < 0
+                      ? 0ull
+                      : static_cast<unsigned long long>(cfg->drain_per_warp > 0 ? cfg->drain_per_warp
+                                                                                 : kDrainPerWarp) *
+                            static_cast<unsigned long long>(nlanes / 32);
   Counters *dc = static_cast<Counters *>(e->counters.p);
   Params<R> P{};
   P.T = S.T;
