@@ -1,10 +1,9 @@
 #include "common.h"
 
 #include <cctype>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
-#include <fstream>
-#include <sstream>
 
 namespace omc {
 
@@ -23,12 +22,23 @@ omc_status fail(omc_status s, const char *fmt, ...) {
 void clear_error() { g_last_error.clear(); }
 
 bool read_file(const std::string &path, std::string &out) {
-  std::ifstream f(path, std::ios::binary);
+  FILE *f = std::fopen(path.c_str(), "rb");
   if (!f) return false;
-  std::ostringstream ss;
-  ss << f.rdbuf();
-  out = ss.str();
-  return true;
+  out.clear();
+  bool ok;
+  long size = std::fseek(f, 0, SEEK_END) == 0 ? std::ftell(f) : -1;
+  if (size >= 0 && std::fseek(f, 0, SEEK_SET) == 0) {  // one read of the whole file
+    out.resize(static_cast<size_t>(size));
+    ok = std::fread(out.data(), 1, out.size(), f) == out.size();
+  } else {  // not seekable: read in blocks
+    std::rewind(f);
+    char buf[1 << 16];
+    size_t n;
+    while ((n = std::fread(buf, 1, sizeof buf, f)) > 0) out.append(buf, n);
+    ok = !std::ferror(f);
+  }
+  std::fclose(f);
+  return ok;
 }
 
 std::vector<std::string> split_lines(const std::string &text) {

@@ -2,6 +2,7 @@
 // output.  Each function restates the reference user-code routine named in
 // its comment; the interaction tables live in media.cpp.
 #include <algorithm>
+#include <cctype>
 #include <charconv>
 #include <cmath>
 #include <cstdlib>
@@ -117,6 +118,67 @@ extern "C" void omc_phantom_free(omc_phantom *ph) {
   std::free(ph);
 }
 
+namespace {
+
+bool is_space(char c) { return std::isspace(static_cast<unsigned char>(c)) != 0; }
+
+// The first n whitespace-separated numbers of [begin, end) (NUL at end) into
+// out, each converted by strtod as fscanf's %lf does; false if the text
+// holds fewer, or a token that is not a number comes first.  Large blocks
+// are cut at whitespace into one piece per thread, parsed in parallel and
+// joined in order, which gives the sequential result.
+bool parse_numbers(const char *begin, const char *end, double *out, size_t n) {
+  const size_t bytes = static_cast<size_t>(end - begin);
+  unsigned hw = std::thread::hardware_concurrency();
+  size_t nthreads = std::max<size_t>(1, std::min<size_t>(hw ? hw : 1, 32));
+  if (bytes < (1u << 20)) nthreads = 1;
+  std::vector<const char *> cut(nthreads + 1, end);
+  cut[0] = begin;
+  for (size_t t = 1; t < nthreads; t++) {
+    const char *c = std::max(cut[t - 1], begin + bytes / nthreads * t);
+    while (c < end && !is_space(*c)) c++;  // a piece never splits a token
+    cut[t] = c;
+  }
+  struct Piece {
+    std::vector<double> v;
+    bool stopped = false;  // a token that is not a number ended the piece
+  };
+  std::vector<Piece> parts(nthreads);
+  auto work = [&](size_t t) {
+    Piece &pc = parts[t];
+    pc.v.reserve(static_cast<size_t>(cut[t + 1] - cut[t]) / 4 + 16);
+    const char *p = cut[t];
+    const char *stop = cut[t + 1];
+    for (;;) {
+      while (p < stop && is_space(*p)) p++;
+      if (p >= stop) return;
+      char *e = nullptr;
+      double x = std::strtod(p, &e);
+      if (e == p) {
+        pc.stopped = true;
+        return;
+      }
+      pc.v.push_back(x);
+      p = e;
+    }
+  };
+  std::vector<std::thread> th;
+  for (size_t t = 1; t < nthreads; t++) th.emplace_back(work, t);
+  work(0);
+  for (auto &t : th) t.join();
+  size_t got = 0;
+  for (const auto &pc : parts) {
+    size_t take = std::min(pc.v.size(), n - got);
+    std::copy(pc.v.begin(), pc.v.begin() + static_cast<std::ptrdiff_t>(take), out + got);
+    got += take;
+    if (got == n) return true;
+    if (pc.stopped) return false;
+  }
+  return false;
+}
+
+}  // namespace
+
 extern "C" omc_status omc_phantom_read(const char *path, omc_phantom **out) {
   if (!path || !out) return fail(OMC_ERR_ARG, "null argument");
   std::string text;
@@ -182,14 +244,13 @@ extern "C" omc_status omc_phantom_read(const char *path, omc_phantom **out) {
     }
     next_line(line);  // blank line
   }
-  // Densities: whitespace-separated numbers in region order.
-  omc::NumberStream ds(text.c_str() + (pos < text.size() ? pos : text.size()));
+  // Densities: whitespace-separated numbers in region order, the first nv
+  // of them.
   size_t nv = static_cast<size_t>(nx) * ny * nz;
-  for (size_t v = 0; v < nv; v++) {
-    if (!ds.next(ph->density[v])) {
-      omc_phantom_free(ph);
-      return fail(OMC_ERR_FORMAT, "%s: truncated density block", path);
-    }
+  if (!parse_numbers(text.c_str() + (pos < text.size() ? pos : text.size()),
+                     text.c_str() + text.size(), ph->density, nv)) {
+    omc_phantom_free(ph);
+    return fail(OMC_ERR_FORMAT, "%s: truncated density block", path);
   }
   for (size_t v = 0; v < nv; v++) {
     if (ph->med_index[v] < 0 || ph->med_index[v] > nmed) {

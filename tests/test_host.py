@@ -62,6 +62,45 @@ def test_egsphant_errors(native, tmp_path):
         api.Phantom.read(str(bad))
 
 
+def _egsphant_text(nx, ny, nz, dens_tokens):
+    rows = "\n".join("1" * nx for _ in range(ny))
+    media = "\n".join(rows + "\n" for _ in range(nz))
+    b = lambda n: " ".join(str(0.5 * i) for i in range(n + 1))
+    return f"1\nH2O700ICRU\n0.25\n{nx} {ny} {nz}\n{b(nx)}\n{b(ny)}\n{b(nz)}\n{media}\n" + dens_tokens
+
+
+def test_egsphant_density_block_parsed_in_pieces(native, tmp_path):
+    """A density block of several MB is cut at whitespace into one piece per
+    thread; the values equal the sequential strtod reading (Python's float
+    is correctly rounded too), trailing text after the last voxel is ignored,
+    and a block that is short, or holds a token that is not a number before
+    its last voxel, is refused as before."""
+    nx, ny, nz = 64, 64, 60
+    nv = nx * ny * nz
+    rng = np.random.default_rng(4)
+    vals = rng.uniform(0.0005, 2.5, nv)
+    toks = [repr(float(v)) if i % 3 else f"{v:.6e}" for i, v in enumerate(vals)]
+    # mixed separators: spaces, tabs, newlines every 7 values
+    body = "".join(t + ("\n" if i % 7 == 6 else (" \t" if i % 5 == 0 else " ")) for i, t in enumerate(toks))
+    path = tmp_path / "big.egsphant"
+    path.write_text(_egsphant_text(nx, ny, nz, body + "\ntrailing words 1.0 x\n"))
+    assert path.stat().st_size > 3 << 20
+    p = api.Phantom.read(str(path))
+    np.testing.assert_array_equal(p.density(), np.array([float(t) for t in toks]).reshape(nz, ny, nx))
+    short = tmp_path / "short.egsphant"
+    short.write_text(_egsphant_text(nx, ny, nz, " ".join(toks[:-1]) + "\n"))
+    with pytest.raises(N.OmcError) as e:
+        api.Phantom.read(str(short))
+    assert e.value.status == 5
+    broken = tmp_path / "broken.egsphant"
+    toks2 = list(toks)
+    toks2[nv // 2] = "abc"
+    broken.write_text(_egsphant_text(nx, ny, nz, " ".join(toks2) + " 1.0\n"))
+    with pytest.raises(N.OmcError) as e:
+        api.Phantom.read(str(broken))
+    assert e.value.status == 5
+
+
 def test_from_arrays_matches_file(native, tmp_path):
     ph = W.slab(n=6, vox=5.0)
     W.write_egsphant(ph, str(tmp_path / "s.egsphant"))
