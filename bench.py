@@ -175,8 +175,9 @@ def run_reference_arm(args, rank):
             "ms_per_step": 1000.0 * tot_s / len(rates), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "histories_per_step": n,
-                       "note": "reference CPU path = oracle port (C restatement, OpenMP, dynamic schedule); "
-                               "the reference's own x86 build cannot run on the aarch64 host"},
+                       "note": "reference CPU path = oracle port (C restatement of the reference, OpenMP, "
+                               "dynamic schedule, bit-exact with the reference's serial build); the reference's "
+                               "own build is compiled from its sources, which this host does not have"},
             "cpu_baseline": {"value": value, "unit": "histories/s", "cores": cores, "kind": "port",
                              "sample": f"{n} histories per step of the workload"},
             "e2e": {"value": value, "unit": "histories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
