@@ -152,8 +152,17 @@ bool parse_numbers(const char *begin, const char *end, double *out, size_t n) {
     for (;;) {
       while (p < stop && is_space(*p)) p++;
       if (p >= stop) return;
+      // from_chars and strtod both round correctly; from_chars is taken
+      // only where it reads the whole token (no '+', hex or range error).
+      double x = 0;
+      auto r = std::from_chars(p, stop, x);
+      if (r.ec == std::errc() && (r.ptr == stop || is_space(*r.ptr))) {
+        pc.v.push_back(x);
+        p = r.ptr;
+        continue;
+      }
       char *e = nullptr;
-      double x = std::strtod(p, &e);
+      x = std::strtod(p, &e);
       if (e == p) {
         pc.stopped = true;
         return;
@@ -162,19 +171,29 @@ bool parse_numbers(const char *begin, const char *end, double *out, size_t n) {
       p = e;
     }
   };
-  std::vector<std::thread> th;
-  for (size_t t = 1; t < nthreads; t++) th.emplace_back(work, t);
-  work(0);
-  for (auto &t : th) t.join();
+  auto run = [nthreads](const auto &fn) {
+    std::vector<std::thread> th;
+    for (size_t t = 1; t < nthreads; t++) th.emplace_back(fn, t);
+    fn(0);
+    for (auto &t : th) t.join();
+  };
+  run(work);
+  // Join in order: piece t supplies values [at[t], at[t] + take[t]).
+  std::vector<size_t> at(nthreads, 0), take(nthreads, 0);
   size_t got = 0;
-  for (const auto &pc : parts) {
-    size_t take = std::min(pc.v.size(), n - got);
-    std::copy(pc.v.begin(), pc.v.begin() + static_cast<std::ptrdiff_t>(take), out + got);
-    got += take;
-    if (got == n) return true;
-    if (pc.stopped) return false;
+  bool ok = false;
+  for (size_t t = 0; t < nthreads && !ok; t++) {
+    at[t] = got;
+    take[t] = std::min(parts[t].v.size(), n - got);
+    got += take[t];
+    if (got == n) ok = true;
+    else if (parts[t].stopped) break;
   }
-  return false;
+  if (!ok) return false;
+  run([&](size_t t) {
+    std::copy(parts[t].v.begin(), parts[t].v.begin() + static_cast<std::ptrdiff_t>(take[t]), out + at[t]);
+  });
+  return true;
 }
 
 }  // namespace

@@ -101,6 +101,23 @@ def test_egsphant_density_block_parsed_in_pieces(native, tmp_path):
     assert e.value.status == 5
 
 
+def test_egsphant_density_tokens_as_fscanf(native, tmp_path):
+    """Tokens read as fscanf %lf reads them: a leading '+', hex floats and
+    exponents with a sign; a token that only starts with a number ends the
+    block."""
+    toks = ["+1.5", "0x1p-1", "2.5E+00", "1e-3", "7", "0.1", "3.25e0", "1E1"]
+    want = [1.5, 0.5, 2.5, 1e-3, 7.0, 0.1, 3.25, 10.0]
+    path = tmp_path / "tok.egsphant"
+    path.write_text(_egsphant_text(2, 2, 2, "\n".join(toks) + "\n1.0x junk\n"))
+    np.testing.assert_array_equal(api.Phantom.read(str(path)).density().reshape(-1), want)
+    path.write_text(_egsphant_text(2, 2, 2, " ".join(toks[:7]) + " 1.0x\n"))
+    a = api.Phantom.read(str(path)).density().reshape(-1)  # "1.0x": strtod reads 1.0
+    np.testing.assert_array_equal(a, want[:7] + [1.0])
+    path.write_text(_egsphant_text(2, 2, 2, " ".join(toks[:6]) + " x 1.0 2.0\n"))
+    with pytest.raises(N.OmcError):
+        api.Phantom.read(str(path))
+
+
 def test_from_arrays_matches_file(native, tmp_path):
     ph = W.slab(n=6, vox=5.0)
     W.write_egsphant(ph, str(tmp_path / "s.egsphant"))
