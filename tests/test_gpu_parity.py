@@ -91,6 +91,24 @@ def test_fp32_against_fp64_on_the_gpu(engine, problem_factory):
     assert abs(c["etot_rel"]) < 0.01, c
 
 
+@pytest.mark.parametrize("precision", [api.FP32, api.FP64])
+def test_drain_mode_does_not_change_the_dose(precision, engine, problem_factory):
+    """The end-of-run drain mode (inline electron interactions, whole
+    tracks per take) only reschedules events.  Forced on from the first
+    iteration (all 400k histories injected at once, threshold far above the
+    in-flight count) it gives the distribution of a run without it."""
+    prob = problem_factory("slab_6mv", ncase=400000, nbatch=50, seeds=(13, 17))
+    engine.load(prob)
+    a, a2, sa = engine.run(precision=precision, drain_per_warp=-1, seeds=(13, 17))
+    b, b2, sb = engine.run(precision=precision, drain_per_warp=1 << 20, seeds=(19, 23))
+    assert sa.error_flags == 0 and sb.error_flags == 0
+    c = compare(a, a2, b, b2, prob.nbatch)
+    assert c["n"] >= 10, c
+    assert consistent(c), c
+    assert abs(c["etot_rel"]) < 6.0 / np.sqrt(400000), c
+    assert sb.ensrc == pytest.approx(sa.ensrc, rel=4.0 / np.sqrt(400000))
+
+
 @pytest.mark.parametrize("schedule", [api.WAVEFRONT, api.LANES])
 def test_energy_balance_closes(engine, problem_factory, schedule):
     """Electrons: all source energy is deposited inside the phantom or
