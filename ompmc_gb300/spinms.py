@@ -37,7 +37,11 @@ NREC_FLOATS = 276
 NENER = 15  # MXE_SPIN (ompmc.h:257)
 NZ = 100
 
-# Header values of the synthetic table (our choice; documented in the design doc).
+# Header values of the synthetic table, chosen here.  The energy grid
+# (1 keV-1 MeV) only sets where the reader interpolates: the rejection
+# function is 1 at every grid point, so it is 1 at every energy.  The
+# screening constant K = 4.25 (z^(2/3) * aux_o, the same for every element)
+# gives etap ~ 1 for H2O700ICRU.
 ESPIN_MIN_KEV = 1.0
 ESPIN_MAX_KEV = 1000.0
 B2SPIN_MAX = 0.99999
