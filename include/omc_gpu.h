@@ -566,7 +566,9 @@ omc_status omc_server_wait(omc_server *s, long long id, double timeout_s,
                            omc_server_result *res);
 
 /* A beamlet job: the dose-influence matrix of bl on job's phantom, as
- * omc_engine_run_dij computes it (job->source gives the spectrum and
+ * omc_engine_run_dij computes it, i.e. the beamlet loop of the matRad front
+ * end (ucodes/omc_matrad/omc_matrad.c:1374-1512) queued on the server
+ * beside field jobs (job->source gives the spectrum and
  * charge; its geometry is the beamlets').  nhist[i] histories for beamlet
  * i, or job->nperbatch * job->nbatch each when nhist is NULL; job->nbatch
  * batches.  All inputs are copied.  The job runs whole, in a turn of its
