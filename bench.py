@@ -131,12 +131,25 @@ def profiled_traffic():
         return None
 
 
-def max_rel_sigma(acc, acc2, nb, frac=0.5):
+def dose_factor(prob):
+    """Per voxel in region order (region 0 left out), the dose that
+    accumulateResults (omc_dosxyz.c:739-799) gives for a batch mean energy of
+    1 MeV: 1.602e-10/(rho V N), and 0 where rho < 0.044.  Energy times it is
+    the dose up to one constant, which is all that a "% of Dmax" selection
+    needs; computed by the library's own accumulateResults."""
+    n = prob.nreg
+    d, _ = prob.dose(np.full(n, 2.0), np.full(n, 2.0), nperbatch=1, nbatch=2)
+    return d[1:]
+
+
+def max_rel_sigma(acc, acc2, nb, factor, frac=0.5):
     """max over voxels with dose > frac*Dmax of the batch relative
-    uncertainty (accumulateResults, omc_dosxyz.c:739-751)."""
+    uncertainty (accumulateResults, omc_dosxyz.c:739-751); `factor` is
+    dose_factor(problem), so the selection is on dose, not energy."""
     m = acc[1:] / nb
     m2 = acc2[1:] / nb
-    sel = m > frac * m.max()
+    d = m * factor
+    sel = d > frac * d.max()
     s = np.sqrt(np.maximum(m2[sel] - m[sel] ** 2, 0.0) / (nb - 1)) / m[sel]
     return float(s.max())
 
@@ -241,7 +254,7 @@ def run_ours(args, rank, world, local_rank, dist_on):
             dev_ms = float(t.item())
         total_hist = world * K * H
         value = total_hist / (dev_ms / 1000.0)
-        s = max_rel_sigma(acc, acc2, K) if K >= 2 else None
+        s = max_rel_sigma(acc, acc2, K, dose_factor(prob)) if K >= 2 else None
         efficiency = 1.0 / (s * s * dev_ms / 1000.0) if s else None
         # plain FP64 path, same workload and job structure, fewer histories
         H64 = FP64_HISTORIES // K
@@ -390,12 +403,13 @@ def run_vrt_leg(args, local_rank):
         prob = build_problem(tmp)
         eng = api.Engine(local_rank).load(prob)
         eng.run(nperbatch=H // 10, nbatch=2, precision=api.FP32)
+        f = dose_factor(prob)
         for ns in (1, 2, 4, 8, 16, 32):
             acc, acc2, st = eng.run(nperbatch=H, nbatch=10, nsplit=ns, precision=api.FP32, seeds=(97, 33 + ns))
             if st.error_flags:
                 raise RuntimeError(f"device error flags {st.error_flags:#x} at nsplit {ns}")
             m, m2 = acc[1:] / 10, acc2[1:] / 10
-            sel = m > 0.5 * m.max()
+            sel = m * f > 0.5 * (m * f).max()
             rel = np.sqrt(np.maximum(m2[sel] - m[sel] ** 2, 0.0) / 9) / m[sel]
             T = st.kernel_ms / 1e3
             out.append({"nsplit": ns, "histories_per_s": 10 * H / T, "T_s": T, "s_max": float(rel.max()),
@@ -444,6 +458,7 @@ def run_ct_leg(args, local_rank):
                             spectrum_file=spec, ncase=H, nbatch=nb, collimator=(-half, half, -half, half), ssd=100.0)
                 prob = api.Problem(api.Input(text=job.text()), phantom=phantom)
                 eng = api.Engine(local_rank).load(prob)
+                f = dose_factor(prob)
                 eng.run(nperbatch=100000, nbatch=1, precision=api.FP32)  # warm-up
                 a32, b32, s32 = eng.run(precision=api.FP32, seeds=(97, 33))
                 a64, b64, s64 = eng.run(precision=api.FP64, seeds=(12, 34))
@@ -451,21 +466,25 @@ def run_ct_leg(args, local_rank):
                 m32, m64 = a32[1:] / nb, a64[1:] / nb
                 v32 = np.maximum(b32[1:] / nb - m32 ** 2, 0) / (nb - 1)
                 v64 = np.maximum(b64[1:] / nb - m64 ** 2, 0) / (nb - 1)
-                # Voxels are selected on the mean of both runs: selecting on one
-                # run alone picks voxels where that run fluctuated upwards.
-                mm = 0.5 * (m32 + m64)
-                sel = mm > 0.2 * mm.max()
+                # Voxels are selected on the dose of the mean of both runs:
+                # selecting on one run alone picks voxels where that run
+                # fluctuated upwards.  The z-scores and ratios below are per
+                # voxel, so energy or dose gives the same values.
+                dm = 0.5 * (m32 + m64) * f
+                sel = dm > 0.2 * dm.max()
                 tz = (m32[sel] - m64[sel]) / np.sqrt(v32[sel] + v64[sel])
                 z = S.norm.ppf(np.clip(S.t.cdf(tz, 2 * (nb - 1)), 1e-300, 1 - 1e-16))
-                hi = mm > 0.5 * mm.max()
+                hi = dm > 0.5 * dm.max()
+                d32, d64 = m32 * f, m64 * f
                 fields.append({"field": f"{gname} {2 * half:g}x{2 * half:g} cm2", "histories": H,
                                "fp32_histories_per_s": H / (s32.kernel_ms / 1e3),
                                "fp64_histories_per_s": H / (s64.kernel_ms / 1e3),
                                "voxels_above_20pct": int(sel.sum()),
                                "frac_within_2sigma": float(np.mean(np.abs(z) <= 2)),
                                "mean_z2": float(np.mean(z * z)),
-                               "dose_rel_diff_above_50pct": float(m32[hi].sum() / m64[hi].sum() - 1),
-                               "sigma_independent_voxels": float(np.sqrt((v32[hi] + v64[hi]).sum()) / m64[hi].sum()),
+                               "dose_rel_diff_above_50pct": float(d32[hi].sum() / d64[hi].sum() - 1),
+                               "sigma_independent_voxels": float(np.sqrt(((v32[hi] + v64[hi]) * f[hi] ** 2).sum())
+                                                                 / d64[hi].sum()),
                                "total_energy_rel_diff": float(a32[1:].sum() / a64[1:].sum() - 1)})
     return {"metric": "FP32-transport dose error vs FP64, per field", "n_gpus": 1, "data": "synthetic",
             "config": {"workload": CT_WORKLOAD, "batches": nb}, "fields": fields}
