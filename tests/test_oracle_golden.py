@@ -10,6 +10,9 @@ import pytest
 from cases import CASES, DIJ_CASES, RANMAR_N, RANMAR_SEEDS, dij_case, write_case
 from conftest import GOLDEN
 
+from ompmc_gb300 import _native as N
+from ompmc_gb300 import workloads as W
+
 
 def test_ranmar_matches_reference_streams(oracle):
     g = np.load(os.path.join(GOLDEN, "ranmar.npz"))
@@ -101,6 +104,48 @@ def test_live_reference_tables_and_dose(oracle, problem_factory, tmp_path):
     a, a2, res = oracle.run(prob, nthreads=1)
     np.testing.assert_array_equal(a, d["accum_endep"])
     np.testing.assert_array_equal(a2, d["accum_endep2"])
+
+
+NINE_MEDIA = ((0.0, 3.0, W.WATER, 1.0), (3.0, 6.0, W.LUNG, 0.26), (6.0, 9.0, W.BONE, 1.85),
+              (9.0, 12.0, W.AIR, 0.0012), (12.0, 15.0, "PMMA700ICRU", 1.19), (15.0, 18.0, "AL700ICRU", 2.7),
+              (18.0, 21.0, "POLYSTY700ICRU", 1.06), (21.0, 24.0, "ICRUTISSUE700ICRU", 1.0),
+              (24.0, 30.0, "TI700ICRU", 4.5))
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(GOLDEN), "..", "oracle", "_ref", "ref_harness")),
+                    reason="reference not built on this machine")
+def test_live_reference_at_the_media_limit(oracle, tmp_path):
+    """Nine media, the reference's MXMED (ompmc.h:358): every table of the
+    host builders equals the reference's, and a serial oracle run equals
+    the reference's batch sums bit for bit.  A tenth medium is refused."""
+    from ompmc_gb300 import api, data
+    from oracle.binding import read_omct
+
+    ph = W.slab(n=12, vox=2.5, layers=NINE_MEDIA)
+    assert len(ph.media) == 9
+    W.write_egsphant(ph, str(tmp_path / "nine.egsphant"))
+    P = data.paths()
+    spec = W.write_spectrum(str(tmp_path / "nine.spectrum"), "synthetic 6 MV", *W.spectrum_6mv())
+    job = W.Job(str(tmp_path / "nine.egsphant"), P["pegs"], P["pgs4form"], P["data_folder"], str(tmp_path) + os.sep,
+                spectrum_file=spec, ncase=600, nbatch=3, seeds=(7, 8), ssd=100.0)
+    inp = job.write(str(tmp_path / "nine"))
+    ref = oracle.ref_tables(inp, str(tmp_path / "ref.bin"))
+    prob = api.Problem.from_file(inp)
+    prob.dump_tables(str(tmp_path / "mine.bin"))
+    mine = read_omct(str(tmp_path / "mine.bin"))
+    for k, v in mine.items():
+        r = ref[k]
+        if k in ("rayleigh.b_array", "rayleigh.c_array"):
+            r, v = r.reshape(-1, 100)[:, :99], v.reshape(-1, 100)[:, :99]
+        np.testing.assert_array_equal(v, r, err_msg=k)
+    d = oracle.ref_dose(inp, str(tmp_path / "dose.bin"))
+    a, a2, _ = oracle.run(prob, nthreads=1)
+    np.testing.assert_array_equal(a, d["accum_endep"])
+    np.testing.assert_array_equal(a2, d["accum_endep2"])
+    ten = list(NINE_MEDIA) + [(30.0, 31.0, "CU700ICRU", 8.9)]
+    ph10 = W.slab(n=12, vox=2.6, layers=tuple(ten))
+    with pytest.raises(N.OmcError):
+        api.Phantom.from_arrays(ph10.media, ph10.xb, ph10.yb, ph10.zb, ph10.med, ph10.rho)
 
 
 def test_oracle_threads_statistically_consistent(oracle, problem_factory):
