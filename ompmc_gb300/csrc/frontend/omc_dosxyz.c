@@ -128,6 +128,10 @@ int main(int argc, char **argv) {
         fprintf(stderr, "'nbatch' must be positive.\n");
         return EXIT_FAILURE;
     }
+    if (nbatch < 2) {  /* accumulateResults divides by nbatch - 1 (omc_dosxyz.c:747) */
+        fprintf(stderr, "'nbatch' must be at least 2: the batch uncertainty divides by nbatch - 1.\n");
+        return EXIT_FAILURE;
+    }
     if (nhist / nbatch == 0) nhist = nbatch;
     long long nperbatch = nhist / nbatch;
     nhist = nperbatch * nbatch;

@@ -46,6 +46,14 @@ def test_missing_key_is_reported(native, tmp_path):
     assert r.returncode != 0 and "phantom file" in r.stderr
 
 
+def test_one_batch_is_refused_before_any_device_call(native, tmp_path):
+    """accumulateResults divides by nbatch - 1; the command line refuses
+    nbatch = 1 right after reading the input, before the engine exists."""
+    inp = write_case("water_mono", str(tmp_path / "one"), ncase=100, nbatch=1)
+    r = subprocess.run([cli(), "-i", inp, "-o", "x"], capture_output=True, text=True, timeout=120)
+    assert r.returncode != 0 and "at least 2" in r.stderr, r.stderr
+
+
 @pytest.mark.gpu
 def test_serial_run_writes_the_reference_3ddose(native, tmp_path):
     """--serial --fp64 follows the reference's serial build: the .3ddose
