@@ -328,44 +328,54 @@ omc_status omc_engine_run_resident(omc_engine *e, const omc_run_config *cfg,
 
 /* ------------------------------------------------------------------------
  * Transport that allocates no device memory.  No counterpart in the
- * reference (which has no GPU path); it exists for callers that cannot
- * call cudaMalloc while they run a dose job: code executing inside a CUDA
- * stream capture or a host callback, where allocation is not allowed,
- * real-time or service code that must not trigger the device-wide
- * synchronisation cudaMalloc/cudaFree may cause, and applications that hand
- * out all device memory from their own pool.
+ * reference (which has no GPU path).  It is for callers that cannot call
+ * cudaMalloc while they run a dose job: applications whose device memory
+ * is all handed out by their own pool or caching allocator (a planning
+ * system that reserves the GPU at start-up, a framework such as PyTorch
+ * that owns the free memory), and services under a fixed device-memory
+ * budget, where a new allocation can fail in mid-job or push other work
+ * out.  The call itself is synchronous: it returns when the transport has
+ * finished, and it reads its counters back to the host.  It is therefore
+ * NOT for use inside a CUDA stream capture or a host callback.
  *
  * omc_engine_run_noalloc transports cfg->nperbatch histories (one batch;
  * cfg->nbatch must be 1) on the per-lane schedule with the tables,
  * geometry and source already resident in the engine, and ADDS the energy
  * deposits (MeV, region order, nx*ny*nz+1 doubles) to d_endep, a DEVICE
- * array the caller owns (zero it first for a fresh tally).  The RANMAR
- * states, particle stacks and counters live in one file-scope device
- * array of fixed size instead of allocated buffers:
+ * array the caller owns.  All its device work runs on `stream` (a
+ * cudaStream_t; NULL is the legacy default stream), after whatever the
+ * caller queued there before, so zero d_endep on that same stream (or
+ * synchronise first) for a fresh tally.  The RANMAR states, particle
+ * stacks and counters live in one file-scope device array of fixed size
+ * instead of allocated buffers:
  *   lanes        cfg->nlanes in 1..OMC_NOALLOC_MAX_LANES (0 = the maximum;
  *                cfg->serial = 1 uses one lane, the reference's serial
  *                build)
- *   stack depth  cfg->stack_depth in 1..OMC_NOALLOC_MAX_DEPTH (0 = maximum)
- * which is OMC_NOALLOC_SCRATCH_BYTES (about 10 MiB) on every GPU that
+ *   stack depth  cfg->stack_depth in 1..OMC_NOALLOC_MAX_DEPTH; 0 takes the
+ *                depth omc_engine_run takes by default, 48 + 4*nsplit,
+ *                which fits only for nsplit <= 4: with stack_depth = 0 a
+ *                larger nsplit is refused (pass an explicit depth; a stack
+ *                that overflows drops histories and returns OMC_ERR_STACK)
+ * which is OMC_NOALLOC_SCRATCH_BYTES (about 19 MiB) on every GPU that
  * loads the library, held until the process exits.  Larger requests are
  * refused with OMC_ERR_ARG.  The first call on a device looks the array's
- * device address up (cudaGetSymbolAddress) with that device current; make
- * that first call before any stream capture.  Every call reuses the same
- * array and leaves its contents behind: the counters are cleared at the
- * start of each call, the streams are re-seeded unless
- * cfg->continue_streams is set (then they continue from the previous
- * no-alloc call with the same lane count).  Calls that overlap on the GPU
- * (several host threads, or several engines on one device) race on the
- * array and must be serialised by the caller.  stats may be NULL; its
- * timing fields are host wall time of the call. */
+ * device address up (cudaGetSymbolAddress) with that device current.
+ * Every call reuses the same array and leaves its contents behind: the
+ * counters are cleared at the start of each call, the streams are
+ * re-seeded unless cfg->continue_streams is set (then they continue from
+ * the previous no-alloc call with the same lane count).  Calls that
+ * overlap on the GPU (several host threads or streams, or several engines
+ * on one device) race on the array and must be serialised by the caller.
+ * stats may be NULL; its timing fields are host wall time of the call. */
 #define OMC_NOALLOC_MAX_LANES 4096
-#define OMC_NOALLOC_MAX_DEPTH 32
+#define OMC_NOALLOC_MAX_DEPTH 64
 #define OMC_NOALLOC_SCRATCH_BYTES                                             \
     ((size_t)OMC_NOALLOC_MAX_LANES * (97 + 3) * 4 +                           \
      (size_t)OMC_NOALLOC_MAX_LANES * OMC_NOALLOC_MAX_DEPTH * (8 * 8 + 4) +    \
      (size_t)256)
 omc_status omc_engine_run_noalloc(omc_engine *e, const omc_run_config *cfg,
-                                  double *d_endep, omc_run_stats *stats);
+                                  double *d_endep, void *stream,
+                                  omc_run_stats *stats);
 
 /* Diagnostics: record, for each iteration of the next wavefront launches
  * (at most `iterations`; 0 switches recording off), the device time in ns

@@ -283,13 +283,26 @@ __host__ __device__ inline void ranmar_seed(int ixx, int jxx, int *u, int stride
   }
 }
 
-// Seed pair of stream k: (ixx, jxx + k), continuing past 31328 into ixx + 1.
+// Seed pair of stream k.  initRandom accepts jxx in 1..31328 but reads it
+// through (jxx/169 % 178, jxx % 169), which has only 30082 distinct values:
+// jxx = 30082 + r gives the same stream as jxx = r.  Stream k is therefore
+// (ixx, jxx + k), the reference's OpenMP thread k (omc_random.c:72), as long
+// as jxx + k <= 30081; past that it continues with the next stream not yet
+// used, into ixx + 1, so that no two of 31328 * 30082 consecutive streams
+// are the same.  Stream 0 is (ixx, jxx) itself.
+constexpr int kJxxStreams = 30082;  // distinct streams per ixx (jxx mod 30082)
 __host__ __device__ inline void stream_seeds(int ixx, int jxx, long long k, int *ik, int *jk) {
   if (ixx <= 0 || ixx > 31328) ixx = 1802;
   if (jxx <= 0 || jxx > 31328) jxx = 9373;
-  long long lin = (long long)(jxx - 1) + k;
-  *jk = (int)(lin % 31328) + 1;
-  *ik = (int)(((long long)(ixx - 1) + lin / 31328) % 31328) + 1;
+  if (k == 0) {
+    *ik = ixx;
+    *jk = jxx;
+    return;
+  }
+  const long long lin = (long long)(jxx % kJxxStreams) + k;
+  const int c = (int)(lin % kJxxStreams);
+  *jk = c == 0 ? kJxxStreams : c;
+  *ik = (int)(((long long)(ixx - 1) + lin / kJxxStreams) % 31328) + 1;
 }
 
 }  // namespace omcgpu

@@ -2009,7 +2009,7 @@ omc_status noalloc_scratch(int device, unsigned char **out) {
 
 template <typename R>
 omc_status run_noalloc(omc_engine *e, PrecisionState<R> &S, const omc_run_config *cfg, int nlanes, int depth,
-                       double *d_endep, omc_run_stats *stats) {
+                       double *d_endep, cudaStream_t stream, omc_run_stats *stats) {
   unsigned char *base = nullptr;
   omc_status s = noalloc_scratch(e->device, &base);
   if (s != OMC_OK) return s;
@@ -2020,14 +2020,18 @@ omc_status run_noalloc(omc_engine *e, PrecisionState<R> &S, const omc_run_config
   Counters *dc = reinterpret_cast<Counters *>(base + kNoallocRngBytes + kNoallocIjcBytes + kNoallocStackBytes +
                                               kNoallocKeyBytes);
   auto t0 = std::chrono::steady_clock::now();
+  // Everything runs on the caller's stream, behind the work the caller
+  // queued there (typically the clearing of d_endep).
   {
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
     if (!(cfg->continue_streams && g_noalloc_lanes[e->device] == nlanes)) {
-      seed_kernel<<<(nlanes + 255) / 256, 256, 0, e->stream>>>(cfg->ixx, cfg->jxx, nlanes, rng_u, rng_ijc);
+      g_noalloc_lanes[e->device] = 0;
+      seed_kernel<<<(nlanes + 255) / 256, 256, 0, stream>>>(cfg->ixx, cfg->jxx, nlanes, rng_u, rng_ijc);
+      CUDA_TRY(cudaGetLastError());
       g_noalloc_lanes[e->device] = nlanes;
     }
   }
-  cudaMemsetAsync(dc, 0, sizeof(Counters), e->stream);  // counters must start at zero
+  CUDA_TRY(cudaMemsetAsync(dc, 0, sizeof(Counters), stream));  // counters must start at zero
   Params<R> P{};
   P.T = S.T;
   P.G = S.G;
@@ -2048,13 +2052,12 @@ omc_status run_noalloc(omc_engine *e, PrecisionState<R> &S, const omc_run_config
   P.n_dep = &dc->n_dep;
   P.max_np = &dc->max_np;
   P.err = &dc->err;
-  transport_kernel<R><<<(nlanes + kBlock - 1) / kBlock, kBlock, kRngSmem, e->stream>>>(P);
-  cudaError_t err = cudaGetLastError();
-  if (err == cudaSuccess) err = cudaStreamSynchronize(e->stream);
-  if (err != cudaSuccess) return fail(OMC_ERR_CUDA, "no-alloc transport: %s", cudaGetErrorString(err));
+  transport_kernel<R><<<(nlanes + kBlock - 1) / kBlock, kBlock, kRngSmem, stream>>>(P);
   Counters hc{};
-  err = cudaMemcpy(&hc, dc, sizeof hc, cudaMemcpyDeviceToHost);
-  if (err != cudaSuccess) return fail(OMC_ERR_CUDA, "no-alloc counters: %s", cudaGetErrorString(err));
+  cudaError_t err = cudaGetLastError();
+  if (err == cudaSuccess) err = cudaMemcpyAsync(&hc, dc, sizeof hc, cudaMemcpyDeviceToHost, stream);
+  if (err == cudaSuccess) err = cudaStreamSynchronize(stream);
+  if (err != cudaSuccess) return fail(OMC_ERR_CUDA, "no-alloc transport: %s", cudaGetErrorString(err));
   double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   if (stats) {
     stats->ensrc = hc.ensrc;
@@ -2076,7 +2079,7 @@ omc_status run_noalloc(omc_engine *e, PrecisionState<R> &S, const omc_run_config
 }  // namespace
 
 extern "C" omc_status omc_engine_run_noalloc(omc_engine *e, const omc_run_config *cfg, double *d_endep,
-                                             omc_run_stats *stats) {
+                                             void *stream, omc_run_stats *stats) {
   if (!e || !cfg || !d_endep) return fail(OMC_ERR_ARG, "null argument");
   if (!e->f64.tables_ok || !e->f64.geom_ok || !e->f64.source_ok)
     return fail(OMC_ERR_STATE, "tables, geometry and source must be set before a run");
@@ -2086,10 +2089,19 @@ extern "C" omc_status omc_engine_run_noalloc(omc_engine *e, const omc_run_config
   int nlanes = cfg->serial ? 1 : (cfg->nlanes > 0 ? cfg->nlanes : OMC_NOALLOC_MAX_LANES);
   if (nlanes > OMC_NOALLOC_MAX_LANES)
     return fail(OMC_ERR_ARG, "nlanes %d exceeds the no-allocation maximum of %d lanes", nlanes, OMC_NOALLOC_MAX_LANES);
-  int depth = cfg->stack_depth > 0 ? cfg->stack_depth : OMC_NOALLOC_MAX_DEPTH;
-  if (depth > OMC_NOALLOC_MAX_DEPTH)
-    return fail(OMC_ERR_ARG, "stack depth %d exceeds the no-allocation maximum of %d", depth, OMC_NOALLOC_MAX_DEPTH);
+  // Default depth: omc_engine_run's, so that a configuration that fits
+  // its stacks there fits them here.
+  const int nsplit = cfg->nsplit < 1 ? 1 : cfg->nsplit;
+  int depth = cfg->stack_depth > 0 ? cfg->stack_depth : kDefaultDepth + 4 * nsplit;
+  if (depth > OMC_NOALLOC_MAX_DEPTH) {
+    if (cfg->stack_depth > 0)
+      return fail(OMC_ERR_ARG, "stack depth %d exceeds the no-allocation maximum of %d", depth, OMC_NOALLOC_MAX_DEPTH);
+    return fail(OMC_ERR_ARG,
+                "nsplit %d needs a stack depth of %d, above the no-allocation maximum of %d (pass stack_depth)",
+                nsplit, depth, OMC_NOALLOC_MAX_DEPTH);
+  }
   if (cudaSetDevice(e->device) != cudaSuccess) return fail(OMC_ERR_CUDA, "cudaSetDevice(%d) failed", e->device);
-  if (cfg->precision == OMC_FP64) return run_noalloc(e, e->f64, cfg, nlanes, depth, d_endep, stats);
-  return run_noalloc(e, e->f32, cfg, nlanes, depth, d_endep, stats);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (cfg->precision == OMC_FP64) return run_noalloc(e, e->f64, cfg, nlanes, depth, d_endep, st, stats);
+  return run_noalloc(e, e->f32, cfg, nlanes, depth, d_endep, st, stats);
 }

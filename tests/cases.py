@@ -101,3 +101,14 @@ def dij_case(name: str, directory: str, ncase: int | None = None, nbatch: int | 
                 pgs4formFile=P["pgs4form"], dataFolder=P["data_folder"], outputFolder=directory + os.sep,
                 relDoseThreshold=thr, verbose=0)
     return inp, ph, bl, opts, thr, job["nsplit"]
+
+
+def run_seeds(i: int, base=(5003, 7)):
+    """Seed pair of repeat i of a run: its lane streams start 2^20 streams
+    after repeat i-1's, so repeats never share a stream (a launch seeds at
+    most about 10^5 lanes).  Adjacent pairs such as (61 + i, 5) would not do:
+    lane k of a run is stream k of its pair, so two such runs share most of
+    their streams."""
+    from ompmc_gb300 import api
+
+    return api.stream_seeds(base[0], base[1], (i + 1) << 20)

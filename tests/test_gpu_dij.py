@@ -8,7 +8,7 @@ import os
 
 import numpy as np
 import pytest
-from cases import DIJ_CASES, dij_case
+from cases import DIJ_CASES, dij_case, run_seeds
 from conftest import GOLDEN
 from stats import compare_runs, consistent
 
@@ -80,7 +80,7 @@ def test_many_lanes_dij_statistically_identical(precision, schedule, engine, ora
 
     def gpu(i):
         col, rows, vals, st = engine.run_dij(rel_threshold=0.0, precision=precision, schedule=schedule,
-                                             seeds=(11 + i, 40 + 3 * i))
+                                             seeds=run_seeds(i))
         assert st.error_flags == 0
         return dense(col, rows, vals, nrows)
 
@@ -106,7 +106,7 @@ def test_uneven_histories_per_beamlet(engine, oracle, dij_problem):
     k = 6
 
     def gpu(i):
-        col, rows, vals, st = engine.run_dij(rel_threshold=0.0, nhist=nh, precision=api.FP32, seeds=(5 + i, 9))
+        col, rows, vals, st = engine.run_dij(rel_threshold=0.0, nhist=nh, precision=api.FP32, seeds=run_seeds(i))
         assert st.histories == nh.sum()
         return dense(col, rows, vals, nrows).sum(axis=1)
 

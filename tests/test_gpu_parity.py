@@ -7,7 +7,7 @@ import os
 
 import numpy as np
 import pytest
-from cases import CASES, RANMAR_N, RANMAR_SEEDS
+from cases import CASES, RANMAR_N, RANMAR_SEEDS, run_seeds
 from conftest import GOLDEN
 from stats import compare, consistent
 
@@ -24,8 +24,8 @@ def test_ranmar_streams_bit_exact(native):
 
 
 def test_ranmar_lane_streams_follow_thread_seeding(native, oracle):
-    # lane k = the reference's OpenMP thread k: seeds (ixx, jxx + k); past
-    # jxx = 31328 the pair continues into ixx + 1.
+    # lane k = stream k of the seed pair (the reference's OpenMP thread k
+    # while jxx + k <= 30081, then the next unused stream).
     out = api.gpu_ranmar(97, 31320, 20, 300)
     for k in range(20):
         ik, jk = api.stream_seeds(97, 31320, k)
@@ -85,7 +85,7 @@ def test_fp32_against_fp64_on_the_gpu(engine, problem_factory):
     prob = problem_factory("slab_6mv", ncase=400000, nbatch=50, seeds=(7, 11))
     engine.load(prob)
     d, d2, _ = engine.run(precision=api.FP64)
-    f, f2, _ = engine.run(precision=api.FP32)
+    f, f2, _ = engine.run(precision=api.FP32, seeds=run_seeds(0))  # streams disjoint from the FP64 run's
     c = compare(f, f2, d, d2, prob.nbatch)
     assert consistent(c), c
     assert abs(c["etot_rel"]) < 0.01, c
@@ -126,7 +126,7 @@ def test_results_independent_of_lane_count(engine, problem_factory):
     prob = problem_factory("water_mono", ncase=200000, nbatch=50, seeds=(3, 4))
     engine.load(prob)
     a, a2, _ = engine.run(precision=api.FP32, nlanes=4096, schedule=api.LANES)
-    b, b2, _ = engine.run(precision=api.FP32, schedule=api.WAVEFRONT)
+    b, b2, _ = engine.run(precision=api.FP32, schedule=api.WAVEFRONT, seeds=run_seeds(1))
     c = compare(a, a2, b, b2, prob.nbatch)
     assert consistent(c) and abs(c["etot_rel"]) < 0.01, c
 

@@ -149,16 +149,17 @@ def column_sums(col, vals):
 
 def test_beamlet_jobs_beside_field_jobs(engine, problem_factory, tmp_path):
     """Beamlet jobs queued among a field job: each gives the dij that
-    omc_engine_run_dij gives (per-beamlet integral doses over 6 jobs against
-    6 engine runs, within their spread), and the field job, whose rounds
-    are cut by the beamlet turns, gives the dose omc_engine_run gives."""
-    from cases import dij_case
+    omc_engine_run_dij gives (per-beamlet integral doses over 16 jobs
+    against 16 engine runs on disjoint streams, within their spread), and
+    the field job, whose rounds are cut by the beamlet turns, gives the dose
+    omc_engine_run gives."""
+    from cases import dij_case, run_seeds
 
     inp, _, bl, _, _, _ = dij_case("dij_slab", str(tmp_path / "d"), ncase=1000, nbatch=2)
     prob = api.Problem.from_file(inp)
     field = problem_factory("slab_6mv", ncase=2000000, nbatch=10, seeds=(3, 4))
     g = lambda key: float(prob.input.get(key))
-    k = 6
+    k = 16
     srv = api.Server(MEDIA, data_text(), precision=api.FP32, round_histories=100000)
     try:
         fid = srv.submit_problem(field)
@@ -185,7 +186,7 @@ def test_beamlet_jobs_beside_field_jobs(engine, problem_factory, tmp_path):
     engine.set_beamlets(bl)
     eng_sums = []
     for i in range(k):
-        col, rows, vals, est = engine.run_dij(rel_threshold=0.0, precision=api.FP32, seeds=(61 + i, 5))
+        col, rows, vals, est = engine.run_dij(rel_threshold=0.0, precision=api.FP32, seeds=run_seeds(i))
         eng_sums.append(column_sums(col, vals))
     eng_sums = np.stack(eng_sums)
     z = (srv_sums.mean(0) - eng_sums.mean(0)) / np.sqrt(srv_sums.var(0, ddof=1) / k + eng_sums.var(0, ddof=1) / k)

@@ -226,13 +226,36 @@ def test_missing_data_file_reported(native, tmp_path):
 
 def test_stream_seed_rule(native):
     # Stream k uses (ixx, jxx + k) like the reference's OpenMP threads
-    # (omc_random.c:72) and continues into ixx + 1 past 31328.
+    # (omc_random.c:72) while jxx + k <= 30081, and then continues with the
+    # next unused stream: initRandom reads jxx through (jxx/169 % 178,
+    # jxx % 169), so jxx = 30082 + r is the stream of jxx = r.
     assert api.stream_seeds(97, 33, 0) == (97, 33)
     assert api.stream_seeds(97, 33, 5) == (97, 38)
-    assert api.stream_seeds(97, 31328, 1) == (98, 1)
-    assert api.stream_seeds(31328, 31328, 1) == (1, 1)
-    pairs = {api.stream_seeds(97, 33, k) for k in range(0, 200000, 7)}
-    assert len(pairs) == len(range(0, 200000, 7))
+    assert api.stream_seeds(97, 30081, 1) == (98, 30082)
+    assert api.stream_seeds(97, 30081, 2) == (98, 1)
+    assert api.stream_seeds(97, 31328, 0) == (97, 31328)
+    assert api.stream_seeds(97, 31328, 1) == (97, 1247)  # 31328 is the stream of 1246
+    assert api.stream_seeds(31328, 30081, 2) == (1, 1)
+    # Distinct streams, not only distinct pairs, over a whole device's lanes
+    # and across jobs placed 2^20 streams apart.
+    def stream(p):
+        return (p[0], p[1] % 30082)
+    ks = list(range(0, 400000, 3)) + [(1 << 20) * j + k for j in range(1, 4) for k in range(0, 100000, 11)]
+    keys = {stream(api.stream_seeds(97, 33, k)) for k in ks}
+    assert len(keys) == len(ks)
+    # Composition: stream k of stream K's pair is stream K + k.
+    for K in (0, 5, 30076, 31328, 1 << 20):
+        for k in (0, 1, 7, 30082):
+            assert stream(api.stream_seeds(*api.stream_seeds(97, 33, K), k)) == stream(api.stream_seeds(97, 33, K + k))
+
+
+def test_ranmar_jxx_alias_is_the_reference_generator(oracle):
+    # The reason for the rule above, on the oracle's generator (the
+    # reference's initRandom): jxx = 30082 + r and jxx = r draw the same
+    # numbers, and the rule's next stream does not.
+    a = oracle.ranmar(97, 31328, 200)
+    assert np.array_equal(a, oracle.ranmar(97, 1246, 200))
+    assert not np.array_equal(oracle.ranmar(*api.stream_seeds(97, 31328, 1), 200), a)
 
 
 def test_3ddose_text_is_printf_byte_for_byte(native, tmp_path, problem_factory):
