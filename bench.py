@@ -35,7 +35,8 @@ sys.path.insert(0, ROOT)
 
 WORKLOAD = "6MV heterogeneous slab 150^3 @ 2 mm, 10x10 cm2 field, SSD 100 cm"
 HISTORIES_PER_STEP = 10_000_000
-FP64_HISTORIES = 4_000_000
+FP64_HISTORIES = 20_000_000  # FP64 job: enough histories for the FP32 dose-error statement
+NSPLIT16_HISTORIES = 10_000_000
 LANES_PER_RANK_STRIDE = 1 << 21  # stream-index stride between ranks (> lanes of one GPU)
 L2_FLUSH_BYTES = 256 << 20       # larger than the 129 MB L2
 
@@ -169,16 +170,71 @@ def cpu_oracle_sample(prob, target_seconds=8.0, cap=5_000_000):
     return n / r.seconds, r.nthreads, n, r.seconds
 
 
+REF_EXE = os.path.join(ROOT, "oracle", "_ref", os.uname().machine, "omc_dosxyz_omp")
+
+
+def reference_sample(exe, tmp, phant, spec, n):
+    """One run of the reference's own OpenMP build (omc_dosxyz, unmodified)
+    on n histories of the workload in 2 batches; returns (transport seconds,
+    threads).  The transport time is the difference of the two "Execution
+    time up to this point" lines the reference prints before and after its
+    batch loop (omc_dosxyz.c:1232-1267): table set-up, phantom parsing and
+    the .3ddose output are outside it."""
+    from ompmc_gb300 import data
+    from ompmc_gb300 import workloads as W
+
+    P = data.paths()
+    job = W.Job(phant, P["pegs"], P["pgs4form"], P["data_folder"], tmp + os.sep, spectrum_file=spec, ncase=n,
+                nbatch=2, collimator=(-5.0, 5.0, -5.0, 5.0), ssd=100.0)
+    inp = job.write(os.path.join(tmp, "ref_job"))
+    out = subprocess.run([exe, "-i", inp, "-o", "ref_job"], capture_output=True, text=True, timeout=600, cwd=tmp)
+    if out.returncode != 0:
+        raise RuntimeError(f"reference exited with {out.returncode}: {out.stdout[-500:]}")
+    times = [float(ln.split(":")[1].split()[0]) for ln in out.stdout.splitlines()
+             if ln.startswith("Execution time up to this point")]
+    threads = [int(ln.split(":")[1]) for ln in out.stdout.splitlines() if ln.startswith("Number of OpenMP threads")]
+    if len(times) < 2:
+        raise RuntimeError("reference output without its timing lines")
+    return times[1] - times[0], (threads[0] if threads else os.cpu_count())
+
+
 def run_reference_arm(args, rank):
+    """The reference's CPU path on this host's cores: its own OpenMP build
+    (oracle/_ref/<arch>/omc_dosxyz_omp, compiled by build() from the
+    reference's sources), else the oracle port when that build is absent."""
     if rank != 0:
         return
+    from ompmc_gb300 import data
+    from ompmc_gb300 import workloads as W
+
     with tempfile.TemporaryDirectory() as tmp:
-        prob = build_problem(tmp)
-        rates, cores, n = [], 0, 0
-        for step in range(args.warmup + args.steps):
-            rate, cores, n, secs = cpu_oracle_sample(prob, target_seconds=4.0)
-            if step >= args.warmup:
-                rates.append((n, secs))
+        data.stage()
+        if os.path.exists(REF_EXE):
+            ph = W.slab(n=150, vox=0.2)
+            phant = W.write_egsphant(ph, os.path.join(tmp, "slab150.egsphant"))
+            spec = W.write_spectrum(os.path.join(tmp, "6mv.spectrum"), "synthetic 6 MV", *W.spectrum_6mv())
+            probe = 200_000
+            secs, cores = reference_sample(REF_EXE, tmp, phant, spec, probe)
+            n = int(min(20_000_000, max(probe, probe / max(secs, 1e-3) * 4.0)))
+            n -= n % 2
+            rates = []
+            for step in range(args.warmup + args.steps):
+                secs, cores = reference_sample(REF_EXE, tmp, phant, spec, n)
+                if step >= args.warmup:
+                    rates.append((n, secs))
+            kind = "reference"
+            note = ("the reference's own omc_dosxyz, unmodified, built from its sources with -O2 -fopenmp "
+                    "(-fcommon) on this host; transport loop time from its own timing lines")
+        else:
+            prob = build_problem(tmp)
+            rates, cores, n = [], 0, 0
+            for step in range(args.warmup + args.steps):
+                rate, cores, n, secs = cpu_oracle_sample(prob, target_seconds=4.0)
+                if step >= args.warmup:
+                    rates.append((n, secs))
+            kind = "port"
+            note = ("oracle port (C restatement of the reference, OpenMP, dynamic schedule, bit-exact with the "
+                    "reference's serial build): the reference's own build is absent on this host")
         tot_n = sum(r[0] for r in rates)
         tot_s = sum(r[1] for r in rates)
         value = tot_n / tot_s
@@ -187,15 +243,57 @@ def run_reference_arm(args, rank):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1000.0 * tot_s / len(rates), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "histories_per_step": n,
-                       "note": "reference CPU path = oracle port (C restatement of the reference, OpenMP, "
-                               "dynamic schedule, bit-exact with the reference's serial build); the reference's "
-                               "own build is compiled from its sources, which this host does not have"},
-            "cpu_baseline": {"value": value, "unit": "histories/s", "cores": cores, "kind": "port",
-                             "sample": f"{n} histories per step of the workload"},
+            "config": {"workload": WORKLOAD, "histories_per_step": n, "note": note},
+            "cpu_baseline": {"value": value, "unit": "histories/s", "cores": cores, "kind": kind,
+                             "sample": f"{n} histories per step of the workload, 2 batches"},
             "e2e": {"value": value, "unit": "histories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         }
         print(json.dumps(line), flush=True)
+
+
+def batch_ratio(a, b):
+    """Relative difference of the batch means of a and b (per-batch values
+    of two runs with the same histories per batch), and its standard error
+    from the spread of the batches of each run."""
+    a, b = np.asarray(a, float), np.asarray(b, float)
+    ma, mb = a.mean(), b.mean()
+    va = a.var(ddof=1) / (len(a) * ma * ma)
+    vb = b.var(ddof=1) / (len(b) * mb * mb)
+    return float(ma / mb - 1.0), float((ma / mb) * np.sqrt(va + vb))
+
+
+def fp32_dose_error(a32, b32, H32, K32, roi32, tot32, a64, b64, H64, K64, roi64, tot64, f, sel20):
+    """FP32-transport dose error against the FP64 run: voxels above 20% of
+    Dmax within 2 combined sigma (batch sigma per voxel, t-corrected to a
+    normal z), mean dose over the voxels above 50% of Dmax and total energy
+    deposited in the phantom, each as a relative difference per history
+    with its standard error from the batch spread of both runs."""
+    from scipy import stats as S
+
+    m32, m64 = a32[1:] / (K32 * H32), a64[1:] / (K64 * H64)  # energy per history
+    v32 = np.maximum(b32[1:] / K32 / H32 ** 2 - m32 ** 2, 0) / (K32 - 1)
+    v64 = np.maximum(b64[1:] / K64 / H64 ** 2 - m64 ** 2, 0) / (K64 - 1)
+    sig = np.sqrt(v32[sel20] + v64[sel20])
+    t = (m32[sel20] - m64[sel20]) / np.where(sig > 0, sig, np.inf)
+    dof = K32 + K64 - 2
+    z = S.norm.ppf(np.clip(S.t.cdf(t, dof), 1e-300, 1 - 1e-16))
+    roi_d, roi_s = batch_ratio(np.asarray(roi32) / H32, np.asarray(roi64) / H64)
+    tot_d, tot_s = batch_ratio(np.asarray(tot32) / H32, np.asarray(tot64) / H64)
+    return {"voxels_above_20pct": int(sel20.sum()), "frac_within_2sigma": float(np.mean(np.abs(z) <= 2.0)),
+            "mean_z2": float(np.mean(z * z)),
+            "dose_rel_diff_above_50pct": roi_d, "dose_rel_diff_sigma": roi_s,
+            "total_energy_rel_diff": tot_d, "total_energy_rel_diff_sigma": tot_s,
+            "histories": {"fp32": K32 * H32, "fp64": K64 * H64}, "batches": {"fp32": K32, "fp64": K64},
+            "sigma": "batch spread of the per-batch region sums of each run, so voxel correlations are included"}
+
+
+def rel_sigmas(acc, acc2, nb, sel):
+    m = acc[1:] / nb
+    m2 = acc2[1:] / nb
+    return np.sqrt(np.maximum(m2[sel] - m[sel] ** 2, 0.0) / (nb - 1)) / m[sel]
+
+
+SERVE_SHORT = dict(jobs=16, rate=2.0, max_histories=2e7, beamlet_frac=0.25, seed=5)
 
 
 def run_ours(args, rank, world, local_rank, dist_on):
@@ -224,15 +322,25 @@ def run_ours(args, rank, world, local_rank, dist_on):
         seeds = D.rank_seeds(97, 33, rank, LANES_PER_RANK_STRIDE)
         H = args.histories_per_step
         K = args.steps
+        f = dose_factor(prob)
         cfg32 = api.Engine.config(H, 1, seeds=seeds, precision=api.FP32, inflight=args.inflight)
-        # warm-up: single batches of the same size
-        for _ in range(args.warmup):
+        # warm-up: single batches of the same size; the last one (host
+        # tallies) also fixes the voxels the dose-error statement uses, so
+        # that they are not selected on the runs they compare
+        for _ in range(args.warmup - 1):
             flush_l2()
             eng.run_resident(cfg32)  # seeds the streams the timed job continues
+        sel_acc, _, _ = eng.run(nperbatch=H, nbatch=1, seeds=seeds, precision=api.FP32, continue_streams=1,
+                                inflight=args.inflight)
+        dsel = sel_acc[1:] * f
+        sel20 = dsel > 0.2 * dsel.max()
+        sel50 = dsel > 0.5 * dsel.max()
+        w_roi = np.concatenate([[0.0], np.where(sel50, f, 0.0)])
+        w_in = np.concatenate([[0.0], np.ones(prob.nreg - 1)])
         # timed region: the K-batch job of K*H histories, FP32 transport /
         # FP64 tallies.  The engine transports all batches of a job in one
-        # launch (batch tallies side by side, 270 MB > L2), so a step is one
-        # of its batches.
+        # launch (batch tallies side by side, > L2), so a step is one of its
+        # batches.
         sampler = ClockSampler(local_rank)
         flush_l2()
         barrier()
@@ -243,6 +351,7 @@ def run_ours(args, rank, world, local_rank, dist_on):
         clocks = sampler.stop()
         if st.error_flags:
             raise RuntimeError(f"device error flags {st.error_flags:#x}")
+        roi32, tot32 = eng.batch_sums(w_roi), eng.batch_sums(w_in)
         dev_ms = float(st.kernel_ms)
         geo, dep, evs = st.voxel_steps, st.deposits, st.steps
         launches = 2  # wavefront transport of all batches, batch accumulation (streams continue: no seeding)
@@ -254,14 +363,38 @@ def run_ours(args, rank, world, local_rank, dist_on):
             dev_ms = float(t.item())
         total_hist = world * K * H
         value = total_hist / (dev_ms / 1000.0)
-        s = max_rel_sigma(acc, acc2, K, dose_factor(prob)) if K >= 2 else None
-        efficiency = 1.0 / (s * s * dev_ms / 1000.0) if s else None
-        # plain FP64 path, same workload and job structure, fewer histories
-        H64 = FP64_HISTORIES // K
-        eng.run(nperbatch=H64 // 4, nbatch=K, seeds=seeds, precision=api.FP64)
+        T = dev_ms / 1000.0
+        s_all = rel_sigmas(acc, acc2, K, sel50) if K >= 2 else None
+        s = float(s_all.max()) if s_all is not None else None
+        efficiency = 1.0 / (s * s * T) if s else None
+        # plain FP64 path, same workload and job structure; enough histories
+        # for the FP32 dose-error statement below
+        K64 = 10
+        H64 = args.fp64_histories // K64
+        eng.run(nperbatch=H64 // 8, nbatch=2, seeds=D.rank_seeds(1201, 77, rank, LANES_PER_RANK_STRIDE),
+                precision=api.FP64)
         flush_l2()
-        _, _, st64 = eng.run(nperbatch=H64, nbatch=K, seeds=seeds, precision=api.FP64)
-        fp64_value = H64 * K / (st64.kernel_ms / 1000.0)
+        a64, b64, st64 = eng.run(nperbatch=H64, nbatch=K64, precision=api.FP64, continue_streams=1)
+        roi64, tot64 = eng.batch_sums(w_roi), eng.batch_sums(w_in)
+        fp64_value = H64 * K64 / (st64.kernel_ms / 1000.0)
+        dose_err = fp32_dose_error(acc, acc2, H, K, roi32, tot32, a64, b64, H64, K64, roi64, tot64, f, sel20)
+        # time to 1% in the voxels above 50% of Dmax: nsplit 1 (the job
+        # above) and nsplit 16 (the best splitting number measured)
+        K16, H16 = 10, args.nsplit16_histories // 10
+        a16, b16, st16 = eng.run(nperbatch=H16, nbatch=K16, nsplit=16, precision=api.FP32,
+                                 seeds=D.rank_seeds(2207, 91, rank, LANES_PER_RANK_STRIDE))
+        T16 = st16.kernel_ms / 1000.0
+        s16 = rel_sigmas(a16, b16, K16, sel50)
+        s_mean = float(s_all.mean()) if s_all is not None else None
+        t1 = {"unit": "s", "target": 0.01, "region": "voxels above 50% of Dmax (dose)",
+              "nsplit1": {"histories": K * H, "T_s": T, "s_max": s, "s_mean": s_mean,
+                          "by_max_s": T * (s / 0.01) ** 2 if s else None,
+                          "by_mean_s": T * (s_mean / 0.01) ** 2 if s_mean else None},
+              "nsplit16": {"histories": K16 * H16, "T_s": T16, "histories_per_s": K16 * H16 / T16,
+                           "s_max": float(s16.max()), "s_mean": float(s16.mean()),
+                           "by_max_s": T16 * (float(s16.max()) / 0.01) ** 2,
+                           "by_mean_s": T16 * (float(s16.mean()) / 0.01) ** 2},
+              "note": "T x (s/0.01)^2: s falls as 1/sqrt(histories); batch sigma (10 batches)"}
         # end to end through the C ABI: phantom upload, the K-batch job,
         # batch sums back in host memory
         ph = prob.phantom
@@ -284,8 +417,13 @@ def run_ours(args, rank, world, local_rank, dist_on):
         # denominator of the tally atomics: scattered FP64 atomicAdd over
         # one batch tally (measured here, after the timed region)
         atomic_peak = api.atomic_rate(prob.nreg)
+        eng.close()
+        del regs
         line = None
         if rank == 0:
+            serving = None
+            if world == 1 and not args.no_serving:
+                serving = run_serve_short(local_rank)
             cpu = None
             if world == 1 and not args.no_cpu_baseline:
                 rate, cores, n, secs = cpu_oracle_sample(prob)
@@ -302,11 +440,14 @@ def run_ours(args, rank, world, local_rank, dist_on):
                            "l2": "flushed before the timed job (256 MB write); the job's batch tallies "
                                  f"({K * prob.nreg * 8 / 1e6:.0f} MB) exceed L2",
                            "parallelism": f"replicas x{world}"},
-                "fp64": {"value": fp64_value, "unit": "histories/s", "histories": H64 * K,
-                         "job": f"{K} batches of {H64} histories in one launch"},
+                "fp64": {"value": fp64_value, "unit": "histories/s", "histories": H64 * K64,
+                         "job": f"{K64} batches of {H64} histories in one launch"},
                 "fp32_over_fp64": value / world / fp64_value,
+                "fp32_dose_error": dose_err,
                 "efficiency": {"value": efficiency, "unit": "1/(s^2*T)", "s_max_rel_above_50pct": s,
-                               "T_s": dev_ms / 1000.0},
+                               "T_s": T},
+                "time_to_1pct": t1,
+                "serving": serving,
                 "job_ms": dev_ms,
                 "per_history": {"events": evs / (K * H), "voxel_steps": geo / (K * H),
                                 "deposits": dep / (K * H), "algorithmic_bytes": per_hist_bytes},
@@ -320,13 +461,14 @@ def run_ours(args, rank, world, local_rank, dist_on):
                                          "peak_kind": "measured live: scattered FP64 atomicAdd over one batch "
                                                       f"tally ({prob.nreg} doubles)"}},
                 "cpu_baseline": cpu,
-                "e2e": {"value": e2e_value, "unit": "histories/s", "h2d_bytes_per_step": int(h2d),
-                        "d2h_bytes_per_step": int(d2h)},
+                "e2e": {"value": e2e_value, "unit": "histories/s", "h2d_bytes_per_step": int(h2d // K),
+                        "d2h_bytes_per_step": int(d2h // K),
+                        "note": f"one job of {K} steps: the phantom ({int(h2d)} B) goes up and the batch sums "
+                                f"({int(d2h)} B) come back once per job, shown here per step; the tables "
+                                "(per medium set, resident across jobs) are uploaded before the timed region"},
                 "gpu_launches": launches,
                 "clocks": clocks,
             }
-        eng.close()
-        del regs
         return line
 
 
@@ -565,7 +707,10 @@ def run_serve_leg(args, local_rank):
         out = {}
         modes = (("continuous", 0, api.Server.SHORTEST_FIRST), ("continuous_equal_shares", 0, api.Server.EQUAL_SHARES),
                  ("one_at_a_time", 1, api.Server.SHORTEST_FIRST))
+        wanted = getattr(args, "serve_modes", None)
         for mode, max_jobs, policy in modes:
+            if wanted and mode not in wanted:
+                continue
             srv = api.Server(media, data_text, precision=api.FP32, max_jobs=max_jobs, policy=policy)
             # warm-up job (tables, kernels)
             srv.wait(srv.submit(phs[0], sources.get((0, 0)) or api.build_source(inputs[0], phs[0]), 0.7, 0.01,
@@ -599,8 +744,25 @@ def run_serve_leg(args, local_rank):
                                            "mean_histories": mean_h, "total_histories": total,
                                            "beamlet_jobs": int(sum(d[3] is not None for d in draws)),
                                            "seed": args.serve_seed},
-                "continuous": out["continuous"], "continuous_equal_shares": out["continuous_equal_shares"],
-                "one_at_a_time": out["one_at_a_time"]}
+                "continuous": out.get("continuous"), "continuous_equal_shares": out.get("continuous_equal_shares"),
+                "one_at_a_time": out.get("one_at_a_time")}
+
+
+def run_serve_short(local_rank):
+    """A short Poisson serving run for the default line: job latency p50/p99
+    and histories/s with continuous batching (the mix of the --serve leg,
+    fewer and smaller jobs)."""
+    ns = argparse.Namespace(serve_seed=SERVE_SHORT["seed"], serve_jobs=SERVE_SHORT["jobs"],
+                            serve_rate=SERVE_SHORT["rate"], serve_max_histories=SERVE_SHORT["max_histories"],
+                            serve_beamlet_frac=SERVE_SHORT["beamlet_frac"], serve_modes=("continuous",))
+    r = run_serve_leg(ns, local_rank)
+    c = r["continuous"]
+    return {"p50_s": c["p50_s"], "p99_s": c["p99_s"], "histories_per_s": c["histories_per_s"],
+            "beamlet_jobs_p50_s": c["beamlet_jobs_p50_s"], "jobs": SERVE_SHORT["jobs"],
+            "rate_per_s": SERVE_SHORT["rate"], "total_histories": r["config"]["total_histories"],
+            "beamlet_jobs": r["config"]["beamlet_jobs"],
+            "workload": "the --serve mix: " + SERVE_WORKLOAD + f"; here {SERVE_SHORT['jobs']} jobs at "
+                        f"{SERVE_SHORT['rate']}/s, histories log-uniform over [1e5, {SERVE_SHORT['max_histories']:.0e}]"}
 
 
 def main():
@@ -612,6 +774,9 @@ def main():
     ap.add_argument("--histories-per-step", type=int, default=HISTORIES_PER_STEP,
                     help="smaller values only for profiler captures of the same code path")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serving", action="store_true", help="leave the short serving run out of the default line")
+    ap.add_argument("--fp64-histories", type=int, default=FP64_HISTORIES)
+    ap.add_argument("--nsplit16-histories", type=int, default=NSPLIT16_HISTORIES)
     ap.add_argument("--inflight", type=int, default=0,
                     help="particles in flight (0 = the engine's default); smaller values only to keep the device "
                          "memory of profiler captures small")

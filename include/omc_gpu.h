@@ -326,6 +326,19 @@ omc_status omc_engine_run_resident(omc_engine *e, const omc_run_config *cfg,
                                    const double **d_accum_endep2,
                                    omc_run_stats *stats);
 
+/* Weighted sums of the batch tallies of the last run: out[b] = sum over
+ * regions r of weights[r] * (energy batch b deposited in r), for the
+ * nbatch batches of that run (written to *nbatch when not NULL; out holds
+ * nbatch doubles).  With weights = dose factor on a region of interest and
+ * 0 elsewhere, the spread of out over the batches is the batch uncertainty
+ * of the region's mean dose, voxel correlations included.  Available after
+ * an omc_engine_run / omc_engine_run_resident whose batches shared one
+ * wavefront launch (the default for nbatch > 1); OMC_ERR_STATE otherwise.
+ * No counterpart in the reference, which scores per voxel only
+ * (accumEndep, omc_dosxyz.c:696-737). */
+omc_status omc_engine_batch_sums(omc_engine *e, const double *weights,
+                                 double *out, int *nbatch);
+
 /* ------------------------------------------------------------------------
  * Transport that allocates no device memory.  No counterpart in the
  * reference (which has no GPU path).  It is for callers that cannot call

@@ -170,6 +170,7 @@ def lib(path: str | None = None):
         "omc_engine_set_source": ([vp, pp(Source_t)], C.c_int),
         "omc_engine_run": ([vp, pp(RunConfig_t), pp(C.c_double), pp(C.c_double), pp(RunStats_t)], C.c_int),
         "omc_engine_run_resident": ([vp, pp(RunConfig_t), pp(vp), pp(vp), pp(RunStats_t)], C.c_int),
+        "omc_engine_batch_sums": ([vp, pp(C.c_double), pp(C.c_double), pp(C.c_int)], C.c_int),
         "omc_engine_run_noalloc": ([vp, pp(RunConfig_t), C.c_void_p, C.c_void_p, pp(RunStats_t)], C.c_int),
         "omc_engine_set_beamlets": ([vp, pp(Beamlets_t)], C.c_int),
         "omc_engine_run_dij": ([vp, pp(RunConfig_t), pp(DijConfig_t), pp(pp(Dij_t)), pp(RunStats_t)], C.c_int),

@@ -232,6 +232,17 @@ class Engine:
         check(N.lib().omc_engine_run_resident(self._h, C.byref(cfg), C.byref(d1), C.byref(d2), C.byref(st)))
         return d1.value, d2.value, st
 
+    def batch_sums(self, weights):
+        """Per-batch weighted sums of the last run's batch tallies
+        (omc_engine_batch_sums): out[b] = sum_r weights[r] * E_b[r]."""
+        w = np.ascontiguousarray(weights, dtype=np.float64)
+        if w.shape != (self._problem.nreg,):
+            raise ValueError(f"weights must have {self._problem.nreg} entries")
+        out = np.zeros(65536)
+        nb = C.c_int()
+        check(N.lib().omc_engine_batch_sums(self._h, _dptr(w), _dptr(out), C.byref(nb)))
+        return out[:nb.value].copy()
+
     def set_beamlets(self, beamlets):
         """Upload a :class:`ompmc_gb300.workloads.Beamlets` set (the
         matRad mcSrc fields)."""

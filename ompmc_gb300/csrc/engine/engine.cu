@@ -674,6 +674,8 @@ struct omc_engine {
   DevBuf multi_slots, multi_first;
   // batch tallies when all batches of a run share one launch
   DevBuf batch_tally, batch_first;
+  int batch_tallies = 0;  // batches whose tallies the last run left in batch_tally (0: none)
+  DevBuf weights, batch_dot;
   // per-iteration trace of the last wavefront launch (diagnostics)
   DevBuf trace;
   int trace_cap = 0;
@@ -1228,7 +1230,7 @@ extern "C" void omc_engine_destroy(omc_engine *e) {
   e->f32.beamlets.clear();
   for (DevBuf *b : {&e->dij_tally, &e->dij_first, &e->dij_beamlet, &e->dij_nhist, &e->dij_max, &e->dij_cnt,
                     &e->dij_off, &e->dij_rows, &e->dij_vals, &e->multi_slots, &e->multi_first, &e->trace,
-                    &e->batch_tally, &e->batch_first, &e->dij_factor})
+                    &e->batch_tally, &e->batch_first, &e->dij_factor, &e->weights, &e->batch_dot})
     b->release();
   cudaStreamDestroy(e->stream);
   delete e;
@@ -1362,6 +1364,7 @@ static omc_status run_batches_one_launch(omc_engine *e, const omc_run_config *cf
   gs.kernel_ms += ms;
   gs.transport_ms += ms;
   if (stats) *stats = gs;
+  e->batch_tallies = nb;
   return s;
 }
 
@@ -1408,6 +1411,7 @@ static omc_status engine_run(omc_engine *e, const omc_run_config *cfg, omc_run_s
   if (s != OMC_OK) return s;
   const bool fp64 = rp.fp64, wavefront = rp.wavefront;
   const int nlanes = rp.nlanes, depth = rp.depth;
+  e->batch_tallies = 0;
   cudaMemsetAsync(e->endep.p, 0, e->nreg * sizeof(double), e->stream);
   cudaMemsetAsync(e->acc.p, 0, e->nreg * sizeof(double), e->stream);
   cudaMemsetAsync(e->acc2.p, 0, e->nreg * sizeof(double), e->stream);
@@ -1474,6 +1478,49 @@ extern "C" omc_status omc_engine_run_resident(omc_engine *e, const omc_run_confi
   if (d_acc) *d_acc = static_cast<const double *>(e->acc.p);
   if (d_acc2) *d_acc2 = static_cast<const double *>(e->acc2.p);
   return s;
+}
+
+// out[b] += sum over regions r of w[r] * tally[b][r].  Grid: x over regions,
+// y over batches.
+__global__ void batch_dot_kernel(const double *__restrict__ tally, long long nreg, const double *__restrict__ w,
+                                 double *out) {
+  __shared__ double part[256 / 32];
+  const double *t = tally + static_cast<size_t>(blockIdx.y) * nreg;
+  double acc = 0.0;
+  for (long long r = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; r < nreg;
+       r += static_cast<long long>(gridDim.x) * blockDim.x)
+    acc += w[r] * t[r];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sum = 0.0;
+    for (int k = 0; k < static_cast<int>(blockDim.x) / 32; k++) sum += part[k];
+    atomicAdd(out + blockIdx.y, sum);
+  }
+}
+
+extern "C" omc_status omc_engine_batch_sums(omc_engine *e, const double *weights, double *out, int *nbatch) {
+  if (!e || !weights || !out) return fail(OMC_ERR_ARG, "null argument");
+  const int nb = e->batch_tallies;
+  if (nb < 1) return fail(OMC_ERR_STATE, "the last run kept no batch tallies (a multi-batch wavefront run does)");
+  omc_status s;
+  if ((s = ensure_device(e)) != OMC_OK) return s;
+  if ((s = e->weights.ensure(static_cast<size_t>(e->nreg) * sizeof(double))) != OMC_OK) return s;
+  if ((s = e->batch_dot.ensure(static_cast<size_t>(nb) * sizeof(double))) != OMC_OK) return s;
+  CUDA_TRY(cudaMemcpyAsync(e->weights.p, weights, static_cast<size_t>(e->nreg) * sizeof(double),
+                           cudaMemcpyHostToDevice, e->stream));
+  CUDA_TRY(cudaMemsetAsync(e->batch_dot.p, 0, static_cast<size_t>(nb) * sizeof(double), e->stream));
+  const int bx = static_cast<int>(std::min<long long>((e->nreg + 255) / 256, std::max(1, 4 * e->nsm / nb + 1)));
+  batch_dot_kernel<<<dim3(bx, nb), 256, 0, e->stream>>>(static_cast<const double *>(e->batch_tally.p), e->nreg,
+                                                        static_cast<const double *>(e->weights.p),
+                                                        static_cast<double *>(e->batch_dot.p));
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemcpyAsync(out, e->batch_dot.p, static_cast<size_t>(nb) * sizeof(double), cudaMemcpyDeviceToHost,
+                           e->stream));
+  CUDA_TRY(cudaStreamSynchronize(e->stream));
+  if (nbatch) *nbatch = nb;
+  return OMC_OK;
 }
 
 // ---------------------------------------------------------------------------

@@ -5,8 +5,8 @@ file, ``pgs4form.dat``, ``xcom_{photo,rayleigh,pair,triplet}.data``,
 ``msnew.data`` and ``spinms.data``.  A user points the ``.inp`` keys at their
 own copies.  For tests and benchmarks the files are staged once into
 ``ompmc_gb300/data/staged/`` (not version controlled) from a reference tree
-given by the ``OMC_REFERENCE_DATA`` environment variable or the default
-location of the read-only reference checkout, and ``spinms.data`` is written
+given by the ``OMC_REFERENCE_DATA`` environment variable, else a checkout
+named ``reference`` beside this repository, and ``spinms.data`` is written
 by :mod:`ompmc_gb300.spinms` because the reference does not ship it.
 """
 
@@ -19,7 +19,7 @@ from . import spinms
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 STAGED = os.path.join(HERE, "data", "staged")
-_DEFAULT_REF = os.path.join(os.sep, "root", "reference")
+_DEFAULT_REF = os.path.normpath(os.path.join(HERE, "..", "..", "reference"))
 
 PEGS_FILES = ("700icru.pegs4dat", "pgs4form.dat")
 DATA_FILES = ("xcom_photo.data", "xcom_rayleigh.data", "xcom_pair.data", "xcom_triplet.data",

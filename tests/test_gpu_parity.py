@@ -11,6 +11,7 @@ from cases import CASES, RANMAR_N, RANMAR_SEEDS, run_seeds
 from conftest import GOLDEN
 from stats import compare, consistent
 
+from ompmc_gb300 import _native as N
 from ompmc_gb300 import api
 
 pytestmark = pytest.mark.gpu
@@ -140,3 +141,28 @@ def test_reproducible_for_fixed_seeds_and_lanes(engine, problem_factory):
     a, _, _ = engine.run(precision=api.FP64, serial=1)
     b, _, _ = engine.run(precision=api.FP64, serial=1)
     np.testing.assert_array_equal(a, b)
+
+
+def test_batch_sums_are_the_batch_tallies_weighted(engine, problem_factory):
+    """omc_engine_batch_sums over the batches of one multi-batch launch: with
+    unit weights inside the phantom they add up to the accumulated total, and
+    the squares of per-region weights add up to the accumulated squares."""
+    prob = problem_factory("slab_6mv", ncase=200000, nbatch=10, seeds=(41, 47))
+    engine.load(prob)
+    a, a2, _ = engine.run(precision=api.FP32)
+    w = np.zeros(prob.nreg)
+    w[1:] = 1.0
+    tot = engine.batch_sums(w)
+    assert len(tot) == prob.nbatch
+    assert tot.sum() == pytest.approx(a[1:].sum(), rel=1e-12)
+    r = int(np.argmax(a))
+    one = np.zeros(prob.nreg)
+    one[r] = 1.0
+    per_batch = engine.batch_sums(one)
+    assert per_batch.sum() == pytest.approx(a[r], rel=1e-12)
+    assert (per_batch ** 2).sum() == pytest.approx(a2[r], rel=1e-12)
+    # One-batch runs keep no batch tallies.
+    engine.run(nbatch=1, precision=api.FP32)
+    with pytest.raises(N.OmcError) as e:
+        engine.batch_sums(w)
+    assert e.value.status == 10
