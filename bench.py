@@ -264,8 +264,8 @@ def batch_ratio(a, b):
 
 def fp32_dose_error(a32, b32, H32, K32, roi32, tot32, a64, b64, H64, K64, roi64, tot64, f, sel20):
     """FP32-transport dose error against the FP64 run: voxels above 20% of
-    Dmax within 2 combined sigma (batch sigma per voxel, t-corrected to a
-    normal z), mean dose over the voxels above 50% of Dmax and total energy
+    Dmax within 2 combined sigma (batch sigma per voxel; the Welch t mapped
+    to a normal z), mean dose over the voxels above 50% of Dmax and total energy
     deposited in the phantom, each as a relative difference per history
     with its standard error from the batch spread of both runs."""
     from scipy import stats as S
@@ -273,9 +273,12 @@ def fp32_dose_error(a32, b32, H32, K32, roi32, tot32, a64, b64, H64, K64, roi64,
     m32, m64 = a32[1:] / (K32 * H32), a64[1:] / (K64 * H64)  # energy per history
     v32 = np.maximum(b32[1:] / K32 / H32 ** 2 - m32 ** 2, 0) / (K32 - 1)
     v64 = np.maximum(b64[1:] / K64 / H64 ** 2 - m64 ** 2, 0) / (K64 - 1)
-    sig = np.sqrt(v32[sel20] + v64[sel20])
+    va, vb = v32[sel20], v64[sel20]
+    sig = np.sqrt(va + vb)
     t = (m32[sel20] - m64[sel20]) / np.where(sig > 0, sig, np.inf)
-    dof = K32 + K64 - 2
+    # Welch-Satterthwaite degrees of freedom per voxel: the two runs have
+    # different history counts, so their batch variances differ.
+    dof = (va + vb) ** 2 / np.maximum(va ** 2 / (K32 - 1) + vb ** 2 / (K64 - 1), 1e-300)
     z = S.norm.ppf(np.clip(S.t.cdf(t, dof), 1e-300, 1 - 1e-16))
     roi_d, roi_s = batch_ratio(np.asarray(roi32) / H32, np.asarray(roi64) / H64)
     tot_d, tot_s = batch_ratio(np.asarray(tot32) / H32, np.asarray(tot64) / H64)

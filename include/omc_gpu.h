@@ -508,6 +508,31 @@ omc_status omc_engine_job_add(omc_engine *e, const omc_phantom *ph,
 /* Histories transported so far / in total. */
 long long omc_job_done(const omc_job *j);
 long long omc_job_histories(const omc_job *j);
+
+/* Beamlet (dij) job resident on the engine: the omc_matrad beamlet loop
+ * (ucodes/omc_matrad/omc_matrad.c:1374-1512) as a job that advances in
+ * rounds beside field jobs.  History k of the job belongs to beamlet b
+ * with sum(nh[0..b-1]) <= k < sum(nh[0..b]) (nh = nhist, or nperbatch *
+ * nbatch for every beamlet when nhist is NULL), starts from that beamlet's
+ * source (initHistory(ibeamlet), :1084-1254) and scores into the beamlet's
+ * own tally; nbatch only divides the dose, as in the reference (:1418).  At
+ * most 4096 beamlets per job.  When the job is done,
+ * omc_engine_job_dij converts its tallies into the CSC dij that
+ * omc_engine_run_dij returns for the same beamlets (values per history,
+ * entries above rel_threshold of each beamlet's maximum).  A beamlet job
+ * is freed with omc_engine_job_remove.  omc_job_dij_device_bytes is its
+ * device footprint. */
+omc_status omc_engine_job_add_dij(omc_engine *e, const omc_phantom *ph,
+                                  const omc_regions *r, const omc_source *src,
+                                  const omc_beamlets *bl,
+                                  const long long *nhist, long long nperbatch,
+                                  int nbatch, int precision, omc_job **out);
+omc_status omc_engine_job_dij(omc_engine *e, omc_job *job,
+                              double rel_threshold, int fp32_values,
+                              omc_dij **out);
+size_t omc_job_dij_device_bytes(const omc_phantom *ph, int nbeamlets,
+                                int precision);
+
 /* One launch over njobs jobs of one precision.  cfg supplies nsplit,
  * inflight and the seeds used when the streams are (re)seeded: streams
  * continue between rounds when cfg->continue_streams is set. */
@@ -594,12 +619,11 @@ omc_status omc_server_wait(omc_server *s, long long id, double timeout_s,
  * beside field jobs (job->source gives the spectrum and
  * charge; its geometry is the beamlets').  nhist[i] histories for beamlet
  * i, or job->nperbatch * job->nbatch each when nhist is NULL; job->nbatch
- * batches.  All inputs are copied.  The job runs whole, in a turn of its
- * own between rounds: when shortest-remaining-first picks it, or with
- * equal shares when it is the oldest resident job.  Its RANMAR streams are
- * the server's, advanced by ((id mod 512) + 1) * 2^20 streams; field
- * rounds after it take streams from (513 + e mod 400) * 2^20 on, for the
- * e-th such reseeding. */
+ * batches; at most 4096 beamlets.  All inputs are copied.  The job is
+ * admitted and scheduled like a field job (omc_engine_job_add_dij): it is
+ * resident with one tally per beamlet, advances in the same rounds (its
+ * histories share launches with the other jobs' histories), and is turned
+ * into its CSC dij on the device when its last history is done. */
 omc_status omc_server_submit_dij(omc_server *s, const omc_server_job *job,
                                  const omc_beamlets *bl,
                                  const long long *nhist, double rel_threshold,

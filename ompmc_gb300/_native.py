@@ -185,6 +185,10 @@ def lib(path: str | None = None):
         "omc_engine_job_round": ([vp, pp(vp), pp(C.c_longlong), C.c_int, pp(RunConfig_t), pp(RunStats_t)],
                                  C.c_int),
         "omc_engine_job_result": ([vp, vp, pp(C.c_double), pp(C.c_double), pp(C.c_double)], C.c_int),
+        "omc_engine_job_add_dij": ([vp, pp(Phantom_t), pp(Regions_t), pp(Source_t), pp(Beamlets_t),
+                                    pp(C.c_longlong), C.c_longlong, C.c_int, C.c_int, pp(vp)], C.c_int),
+        "omc_engine_job_dij": ([vp, vp, C.c_double, C.c_int, pp(pp(Dij_t))], C.c_int),
+        "omc_job_dij_device_bytes": ([pp(Phantom_t), C.c_int, C.c_int], C.c_size_t),
         "omc_engine_job_remove": ([vp, vp], None),
         "omc_server_create": ([pp(ServerConfig_t), vp, C.c_int, pp(C.c_char_p), pp(vp)], C.c_int),
         "omc_server_submit": ([vp, pp(ServerJob_t), pp(C.c_longlong)], C.c_int),

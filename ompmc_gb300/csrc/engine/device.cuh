@@ -153,20 +153,25 @@ struct Source {
 };
 
 // One resident dose job of a multi-job launch: its own phantom, source,
-// per-batch tallies and source-energy sum.  History k of the job (counted
-// over all launches) belongs to batch k / nperbatch.
+// tallies and source-energy sum.  Field jobs: history k of the job
+// (counted over all launches) scores in batch k / nperbatch.  Beamlet
+// (dij) jobs: history k belongs to the beamlet b with bl_first[b] <= k <
+// bl_first[b+1], starts from that beamlet's source, and scores in tally b.
 template <typename R>
 struct JobSlot {
   Geometry<R> G;
   Source<R> S;
-  double *tally;        // [nbatch][nreg]
+  double *tally;        // [nbatch][nreg], beamlet jobs [nbl][nreg]
   double *ensrc;        // [1]
   long long nreg;
   long long h0;         // job history index of this launch's first history
   long long nperbatch;
+  const long long *bl_first;  // beamlet jobs: [nbl + 1] first job history of each beamlet
+  int nbl;                    // beamlets (0: field job)
 };
 
-// Queue tag of a particle in a multi-job launch: job slot and batch.
+// Queue tag of a particle in a multi-job launch: job slot and batch (or
+// beamlet).
 constexpr int kBatchTag = 4096;
 
 template <typename R>

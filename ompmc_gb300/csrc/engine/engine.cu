@@ -1569,6 +1569,84 @@ void add_stats(omc_run_stats &acc, const omc_run_stats &g) {
   acc.warnings |= g.warnings;
 }
 
+// Dose, threshold and CSC columns of ng beamlet tallies [ng][nreg] (the
+// beamlet's energy summed over its nbatch batches): dose in place in the
+// reference's operation order (omc_matrad.c:839-919), entries above
+// rel * the beamlet's maximum, appended to out as columns g0..g0+ng-1 (the
+// host arrays grow; host_cap is their capacity).  nh: histories of each of
+// the ng beamlets.
+omc_status dij_group_to_csc(omc_engine *e, double *tally, int ng, long long nreg, int nx, int ny, const double *xb,
+                            const double *yb, const double *zb, const double *density, const long long *nh,
+                            int nbatch, double rel, bool f32v, omc_dij *out, int g0, long long &host_cap) {
+  omc_status s;
+  const long long nvox = nreg - 1;
+  const int ntiles = static_cast<int>((nvox + kDijTile - 1) / kDijTile);
+  const size_t vsize = f32v ? sizeof(float) : sizeof(double);
+  if ((s = e->dij_nhist.ensure(ng * sizeof(double))) != OMC_OK) return s;
+  if ((s = e->dij_max.ensure(ng * sizeof(unsigned long long))) != OMC_OK) return s;
+  if ((s = e->dij_cnt.ensure(static_cast<size_t>(ng) * ntiles * sizeof(long long))) != OMC_OK) return s;
+  if ((s = e->dij_off.ensure((static_cast<size_t>(ng) * ntiles + 1) * sizeof(long long))) != OMC_OK) return s;
+  if ((s = e->dij_factor.ensure(static_cast<size_t>(nvox) * sizeof(double))) != OMC_OK) return s;
+  std::vector<double> nhd(ng);
+  std::vector<long long> tile0(ng);
+  for (int i = 0; i < ng; i++) nhd[i] = 1.0 / static_cast<double>(nh[i]);  // per-slot 1/nhist (uneven counts)
+  CUDA_TRY(cudaMemcpyAsync(e->dij_nhist.p, nhd.data(), ng * sizeof(double), cudaMemcpyHostToDevice, e->stream));
+  CUDA_TRY(cudaMemsetAsync(e->dij_max.p, 0, ng * sizeof(unsigned long long), e->stream));
+  auto *smax = static_cast<unsigned long long *>(e->dij_max.p);
+  auto *cnt = static_cast<long long *>(e->dij_cnt.p);
+  auto *off = static_cast<long long *>(e->dij_off.p);
+  // Per-voxel factor; the group's history count goes into it when every
+  // beamlet of the group has the same count (the reference's case, bit
+  // for bit), else each slot applies its own 1/nhist.
+  bool uniform = true;
+  for (int i = 1; i < ng; i++) uniform = uniform && nh[i] == nh[0];
+  double *factor = static_cast<double *>(e->dij_factor.p);
+  dij_factor_kernel<<<static_cast<int>(std::min<long long>((nvox + 255) / 256, 16 * e->nsm)), 256, 0, e->stream>>>(
+      nvox, nx, ny, xb, yb, zb, density, uniform ? static_cast<double>(nh[0]) : 0.0, factor);
+  const int bx = static_cast<int>(std::min<long long>((nvox + 255) / 256, std::max(4, 64 * e->nsm / ng + 1)));
+  dij_dose_kernel<<<dim3(bx, ng), 256, 0, e->stream>>>(tally, nreg, factor, nbatch, smax);
+  dij_count_kernel<<<dim3(ntiles, ng), kDijThreads, 0, e->stream>>>(tally, nreg, ntiles, smax, rel, cnt);
+  const long long ncnt = static_cast<long long>(ng) * ntiles;
+  dij_scan_kernel<<<1, 1024, 0, e->stream>>>(cnt, ncnt, off);
+  long long gnnz = 0;
+  CUDA_TRY(cudaMemcpyAsync(&gnnz, off + ncnt, sizeof gnnz, cudaMemcpyDeviceToHost, e->stream));
+  CUDA_TRY(cudaStreamSynchronize(e->stream));
+  if ((s = e->dij_rows.ensure((gnnz ? gnnz : 1) * sizeof(int))) != OMC_OK) return s;
+  if ((s = e->dij_vals.ensure((gnnz ? gnnz : 1) * vsize)) != OMC_OK) return s;
+  dij_fill_kernel<<<dim3(ntiles, ng), kDijThreads, 0, e->stream>>>(
+      tally, nreg, ntiles, smax, rel, off, uniform ? nullptr : static_cast<const double *>(e->dij_nhist.p),
+      static_cast<int *>(e->dij_rows.p), f32v ? nullptr : static_cast<double *>(e->dij_vals.p),
+      f32v ? static_cast<float *>(e->dij_vals.p) : nullptr);
+  // Column starts: the offset of each slot's first tile.
+  CUDA_TRY(cudaMemcpy2DAsync(tile0.data(), sizeof(long long), off, static_cast<size_t>(ntiles) * sizeof(long long),
+                             sizeof(long long), ng, cudaMemcpyDeviceToHost, e->stream));
+  if (out->nnz + gnnz > host_cap) {
+    long long cap = std::max(out->nnz + gnnz, 2 * host_cap);
+    int *r = static_cast<int *>(std::realloc(out->row_idx, (cap ? cap : 1) * sizeof(int)));
+    if (r) out->row_idx = r;
+    void *v = std::realloc(f32v ? static_cast<void *>(out->values_f32) : static_cast<void *>(out->values),
+                           (cap ? cap : 1) * vsize);
+    if (v) {
+      if (f32v) out->values_f32 = static_cast<float *>(v);
+      else out->values = static_cast<double *>(v);
+    }
+    if (!r || !v) return fail(OMC_ERR_NOMEM, "host allocation of %lld dij entries failed", cap);
+    host_cap = cap;
+  }
+  if (gnnz > 0) {
+    CUDA_TRY(cudaMemcpyAsync(out->row_idx + out->nnz, e->dij_rows.p, gnnz * sizeof(int), cudaMemcpyDeviceToHost,
+                             e->stream));
+    void *vdst = f32v ? static_cast<void *>(out->values_f32 + out->nnz) : static_cast<void *>(out->values + out->nnz);
+    CUDA_TRY(cudaMemcpyAsync(vdst, e->dij_vals.p, gnnz * vsize, cudaMemcpyDeviceToHost, e->stream));
+  }
+  CUDA_TRY(cudaStreamSynchronize(e->stream));
+  CUDA_TRY(cudaGetLastError());
+  for (int i = 0; i < ng; i++) out->col_ptr[g0 + i] = out->nnz + tile0[i];
+  out->nnz += gnnz;
+  out->col_ptr[g0 + ng] = out->nnz;
+  return OMC_OK;
+}
+
 omc_status run_dij(omc_engine *e, const omc_run_config *cfg, const omc_dij_config *dc, omc_dij *out,
                    omc_run_stats *stats) {
   RunPlan rp;
@@ -1594,15 +1672,9 @@ omc_status run_dij(omc_engine *e, const omc_run_config *cfg, const omc_dij_confi
   if (G < 1) G = 1;
   if (G > nb) G = nb;
   if (G > 65535) G = 65535;
-  const int ntiles = static_cast<int>((nvox + kDijTile - 1) / kDijTile);
   if ((s = e->dij_tally.ensure(static_cast<size_t>(G) * slot_bytes)) != OMC_OK) return s;
   if ((s = e->dij_first.ensure((G + 1) * sizeof(long long))) != OMC_OK) return s;
   if ((s = e->dij_beamlet.ensure(G * sizeof(int))) != OMC_OK) return s;
-  if ((s = e->dij_nhist.ensure(G * sizeof(double))) != OMC_OK) return s;
-  if ((s = e->dij_max.ensure(G * sizeof(unsigned long long))) != OMC_OK) return s;
-  if ((s = e->dij_cnt.ensure(static_cast<size_t>(G) * ntiles * sizeof(long long))) != OMC_OK) return s;
-  if ((s = e->dij_off.ensure((static_cast<size_t>(G) * ntiles + 1) * sizeof(long long))) != OMC_OK) return s;
-  if ((s = e->dij_factor.ensure(static_cast<size_t>(nvox) * sizeof(double))) != OMC_OK) return s;
 
   out->nrows = static_cast<int>(nvox);
   out->ncols = nb;
@@ -1610,28 +1682,24 @@ omc_status run_dij(omc_engine *e, const omc_run_config *cfg, const omc_dij_confi
   out->col_ptr = static_cast<long long *>(std::calloc(static_cast<size_t>(nb) + 1, sizeof(long long)));
   if (!out->col_ptr) return fail(OMC_ERR_NOMEM, "host allocation failed");
   const bool f32v = dc->fp32_values != 0;
-  const size_t vsize = f32v ? sizeof(float) : sizeof(double);
   long long host_cap = 0;
   omc_run_stats total{};
   omc_status worst = OMC_OK;
   const double *xb = static_cast<const double *>(e->f64.G.xb), *yb = e->f64.G.yb, *zb = e->f64.G.zb;
-  std::vector<long long> first(G + 1), tile0(G);
+  std::vector<long long> first(G + 1);
   std::vector<int> bl(G);
-  std::vector<double> nhd(G);
   for (int g0 = 0; g0 < nb; g0 += static_cast<int>(G)) {
     const int ng = static_cast<int>(std::min<long long>(G, nb - g0));
     first[0] = 0;
     for (int i = 0; i < ng; i++) {
       first[i + 1] = first[i] + nh[g0 + i];
       bl[i] = g0 + i;
-      nhd[i] = 1.0 / static_cast<double>(nh[g0 + i]);  // per-slot 1/nhist (uneven counts)
     }
-    cudaMemcpyAsync(e->dij_first.p, first.data(), (ng + 1) * sizeof(long long), cudaMemcpyHostToDevice, e->stream);
-    cudaMemcpyAsync(e->dij_beamlet.p, bl.data(), ng * sizeof(int), cudaMemcpyHostToDevice, e->stream);
-    cudaMemcpyAsync(e->dij_nhist.p, nhd.data(), ng * sizeof(double), cudaMemcpyHostToDevice, e->stream);
-    cudaMemsetAsync(e->dij_tally.p, 0, static_cast<size_t>(ng) * slot_bytes, e->stream);
-    cudaMemsetAsync(e->dij_max.p, 0, ng * sizeof(unsigned long long), e->stream);
-    cudaMemsetAsync(e->counters.p, 0, sizeof(Counters), e->stream);
+    CUDA_TRY(cudaMemcpyAsync(e->dij_first.p, first.data(), (ng + 1) * sizeof(long long), cudaMemcpyHostToDevice,
+                             e->stream));
+    CUDA_TRY(cudaMemcpyAsync(e->dij_beamlet.p, bl.data(), ng * sizeof(int), cudaMemcpyHostToDevice, e->stream));
+    CUDA_TRY(cudaMemsetAsync(e->dij_tally.p, 0, static_cast<size_t>(ng) * slot_bytes, e->stream));
+    CUDA_TRY(cudaMemsetAsync(e->counters.p, 0, sizeof(Counters), e->stream));
     SlotJob job{ng, static_cast<const long long *>(e->dij_first.p), static_cast<const int *>(e->dij_beamlet.p),
                 static_cast<double *>(e->dij_tally.p), first[ng], nullptr};
     omc_run_stats gs{};
@@ -1642,62 +1710,10 @@ omc_status run_dij(omc_engine *e, const omc_run_config *cfg, const omc_dij_confi
     add_stats(total, gs);
     if (s != OMC_OK && s != OMC_ERR_STACK && s != OMC_ERR_LIMIT) return s;
     if (s != OMC_OK) worst = s;
-    // Dose, threshold, compaction.
-    double *tally = static_cast<double *>(e->dij_tally.p);
-    auto *smax = static_cast<unsigned long long *>(e->dij_max.p);
-    auto *cnt = static_cast<long long *>(e->dij_cnt.p);
-    auto *off = static_cast<long long *>(e->dij_off.p);
-    // Per-voxel factor; the group's history count goes into it when every
-    // beamlet of the group has the same count (the reference's case, bit
-    // for bit), else each slot applies its own 1/nhist.
-    bool uniform = true;
-    for (int i = 1; i < ng; i++) uniform = uniform && nh[g0 + i] == nh[g0];
-    double *factor = static_cast<double *>(e->dij_factor.p);
-    dij_factor_kernel<<<static_cast<int>(std::min<long long>((nvox + 255) / 256, 16 * e->nsm)), 256, 0, e->stream>>>(
-        nvox, e->f64.G.nx, e->f64.G.ny, xb, yb, zb, static_cast<const double *>(e->density.p),
-        uniform ? static_cast<double>(nh[g0]) : 0.0, factor);
-    const int bx = static_cast<int>(std::min<long long>((nvox + 255) / 256, std::max(4, 64 * e->nsm / ng + 1)));
-    dij_dose_kernel<<<dim3(bx, ng), 256, 0, e->stream>>>(tally, nreg, factor, cfg->nbatch, smax);
-    dij_count_kernel<<<dim3(ntiles, ng), kDijThreads, 0, e->stream>>>(tally, nreg, ntiles, smax, dc->rel_threshold,
-                                                                      cnt);
-    const long long ncnt = static_cast<long long>(ng) * ntiles;
-    dij_scan_kernel<<<1, 1024, 0, e->stream>>>(cnt, ncnt, off);
-    long long gnnz = 0;
-    CUDA_TRY(cudaMemcpyAsync(&gnnz, off + ncnt, sizeof gnnz, cudaMemcpyDeviceToHost, e->stream));
-    CUDA_TRY(cudaStreamSynchronize(e->stream));
-    if ((s = e->dij_rows.ensure((gnnz ? gnnz : 1) * sizeof(int))) != OMC_OK) return s;
-    if ((s = e->dij_vals.ensure((gnnz ? gnnz : 1) * vsize)) != OMC_OK) return s;
-    dij_fill_kernel<<<dim3(ntiles, ng), kDijThreads, 0, e->stream>>>(
-        tally, nreg, ntiles, smax, dc->rel_threshold, off,
-        uniform ? nullptr : static_cast<const double *>(e->dij_nhist.p), static_cast<int *>(e->dij_rows.p),
-        f32v ? nullptr : static_cast<double *>(e->dij_vals.p), f32v ? static_cast<float *>(e->dij_vals.p) : nullptr);
-    // Column starts: the offset of each slot's first tile.
-    CUDA_TRY(cudaMemcpy2DAsync(tile0.data(), sizeof(long long), off, static_cast<size_t>(ntiles) * sizeof(long long),
-                               sizeof(long long), ng, cudaMemcpyDeviceToHost, e->stream));
-    if (out->nnz + gnnz > host_cap) {
-      long long cap = std::max(out->nnz + gnnz, 2 * host_cap);
-      int *r = static_cast<int *>(std::realloc(out->row_idx, (cap ? cap : 1) * sizeof(int)));
-      if (r) out->row_idx = r;
-      void *v = std::realloc(f32v ? static_cast<void *>(out->values_f32) : static_cast<void *>(out->values),
-                             (cap ? cap : 1) * vsize);
-      if (v) {
-        if (f32v) out->values_f32 = static_cast<float *>(v);
-        else out->values = static_cast<double *>(v);
-      }
-      if (!r || !v) return fail(OMC_ERR_NOMEM, "host allocation of %lld dij entries failed", cap);
-      host_cap = cap;
-    }
-    if (gnnz > 0) {
-      CUDA_TRY(cudaMemcpyAsync(out->row_idx + out->nnz, e->dij_rows.p, gnnz * sizeof(int), cudaMemcpyDeviceToHost,
-                               e->stream));
-      void *vdst = f32v ? static_cast<void *>(out->values_f32 + out->nnz) : static_cast<void *>(out->values + out->nnz);
-      CUDA_TRY(cudaMemcpyAsync(vdst, e->dij_vals.p, gnnz * vsize, cudaMemcpyDeviceToHost, e->stream));
-    }
-    CUDA_TRY(cudaStreamSynchronize(e->stream));
-    CUDA_TRY(cudaGetLastError());
-    for (int i = 0; i < ng; i++) out->col_ptr[g0 + i] = out->nnz + tile0[i];
-    out->nnz += gnnz;
-    out->col_ptr[g0 + ng] = out->nnz;
+    if ((s = dij_group_to_csc(e, static_cast<double *>(e->dij_tally.p), ng, nreg, e->f64.G.nx, e->f64.G.ny, xb, yb,
+                              zb, static_cast<const double *>(e->density.p), nh.data() + g0, cfg->nbatch,
+                              dc->rel_threshold, f32v, out, g0, host_cap)) != OMC_OK)
+      return s;
   }
   if (stats) *stats = total;
   if (worst == OMC_ERR_STACK) return fail(OMC_ERR_STACK, "particle stack or queue overflow; histories were dropped");
@@ -1733,11 +1749,17 @@ struct omc_job {
   long long nperbatch = 0, nhist = 0, done = 0;
   int nbatch = 0;
   long long nreg = 0;
-  PrecisionState<float> s32;   // geometry + source when precision is FP32
+  PrecisionState<float> s32;   // geometry + source (+ beamlets) when precision is FP32
   PrecisionState<double> s64;  // ... FP64
-  DevBuf tally;                // [nbatch][nreg]
+  DevBuf tally;                // [nbatch][nreg], beamlet jobs [nbl][nreg]
   DevBuf ensrc;                // [1]
-  DevBuf result;               // [2][nreg] batch sum and sum of squares
+  DevBuf result;               // [2][nreg] batch sum and sum of squares (field jobs)
+  // beamlet (dij) jobs
+  int nbl = 0;
+  int nx = 0, ny = 0;
+  std::vector<long long> nh;   // histories of each beamlet
+  DevBuf bl_first;             // [nbl + 1]
+  DevBuf density, bounds;      // FP64 densities [nvox] and x/y/z bounds, for the dose conversion
 };
 
 namespace {
@@ -1755,6 +1777,14 @@ JobSlot<R> job_slot(const PrecisionState<R> &S, omc_job *j) {
   js.nreg = j->nreg;
   js.h0 = j->done;
   js.nperbatch = j->nperbatch;
+  js.nbl = j->nbl;
+  js.bl_first = static_cast<const long long *>(j->bl_first.p);
+  if (j->nbl > 0) {
+    js.S.beamlets = 1;
+    js.S.bixel = S.bixel;
+    js.S.beam_src = S.beam_src;
+    js.S.ibeam = S.ibeam;
+  }
   return js;
 }
 
@@ -1838,6 +1868,117 @@ extern "C" omc_status omc_engine_job_add(omc_engine *e, const omc_phantom *ph, c
   CUDA_TRY(cudaMemset(j->tally.p, 0, static_cast<size_t>(nbatch) * j->nreg * sizeof(double)));
   CUDA_TRY(cudaMemset(j->ensrc.p, 0, sizeof(double)));
   *out = j.release();
+  return OMC_OK;
+}
+
+extern "C" size_t omc_job_dij_device_bytes(const omc_phantom *ph, int nbeamlets, int precision) {
+  if (!ph) return 0;
+  size_t nreg = static_cast<size_t>(ph->nx) * ph->ny * ph->nz + 1;
+  size_t rsize = precision == OMC_FP32 ? 4 : 8;
+  return nreg * (1 + rsize) + nreg * 8 * (static_cast<size_t>(nbeamlets > 0 ? nbeamlets : 1) + 1) +
+         (static_cast<size_t>(ph->nx + ph->ny + ph->nz + 3) + 2 * OMC_INVDIM) * (rsize + 8) +
+         static_cast<size_t>(nbeamlets > 0 ? nbeamlets : 1) * (9 * rsize + 12) + 4096;
+}
+
+extern "C" omc_status omc_engine_job_add_dij(omc_engine *e, const omc_phantom *ph, const omc_regions *r,
+                                             const omc_source *src, const omc_beamlets *bl, const long long *nhist,
+                                             long long nperbatch, int nbatch, int precision, omc_job **out) {
+  if (!e || !ph || !r || !src || !bl || !out) return fail(OMC_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (!e->f64.tables_ok) return fail(OMC_ERR_STATE, "omc_engine_set_tables must come first");
+  if (bl->nbeamlets < 1 || bl->nbeamlets > kBatchTag || bl->nbeams < 1)
+    return fail(OMC_ERR_ARG, "need 1 to %d beamlets and at least one beam", kBatchTag);
+  if (nbatch < 1) return fail(OMC_ERR_ARG, "need nbatch >= 1");
+  if (precision != OMC_FP32 && precision != OMC_FP64) return fail(OMC_ERR_ARG, "unknown precision");
+  for (int i = 0; i < bl->nbeamlets; i++) {
+    if (bl->ibeam[i] < 0 || bl->ibeam[i] >= bl->nbeams) return fail(OMC_ERR_ARG, "beamlet %d: bad beam", i);
+    const long long h = nhist ? nhist[i] : nperbatch * nbatch;
+    if (h < 1) return fail(OMC_ERR_ARG, "beamlet %d: history count %lld must be >= 1", i, h);
+  }
+  int nmed = e->host_tables_dims.nmed;
+  RegionData rd;
+  omc_status s;
+  if ((s = region_data(nmed, ph, r, rd)) != OMC_OK) return s;
+  if ((s = ensure_device(e)) != OMC_OK) return s;
+  std::unique_ptr<omc_job> j(new omc_job());
+  j->precision = precision;
+  j->nbatch = nbatch;
+  j->nbl = bl->nbeamlets;
+  j->nreg = r->nreg;
+  j->nx = ph->nx;
+  j->ny = ph->ny;
+  j->nh.resize(j->nbl);
+  std::vector<long long> first(j->nbl + 1, 0);
+  for (int i = 0; i < j->nbl; i++) {
+    j->nh[i] = nhist ? nhist[i] : nperbatch * nbatch;
+    first[i + 1] = first[i] + j->nh[i];
+  }
+  j->nhist = first[j->nbl];
+  j->nperbatch = j->nhist;  // one "batch" range: the beamlet decides the tally
+  if (precision == OMC_FP32) {
+    if ((s = upload_geometry(j->s32, ph, rd.med, rd.rhof, rd.ecut_m.data(), rd.pcut_m.data(), nmed)) != OMC_OK)
+      return s;
+    if ((s = upload_source(j->s32, src)) != OMC_OK) return s;
+    if ((s = upload_beamlets(j->s32, bl)) != OMC_OK) return s;
+  } else {
+    if ((s = upload_geometry(j->s64, ph, rd.med, rd.rhof, rd.ecut_m.data(), rd.pcut_m.data(), nmed)) != OMC_OK)
+      return s;
+    if ((s = upload_source(j->s64, src)) != OMC_OK) return s;
+    if ((s = upload_beamlets(j->s64, bl)) != OMC_OK) return s;
+  }
+  const size_t nvox = static_cast<size_t>(j->nreg - 1);
+  const size_t nb = static_cast<size_t>(ph->nx + 1) + (ph->ny + 1) + (ph->nz + 1);
+  if ((s = j->tally.ensure(static_cast<size_t>(j->nbl) * j->nreg * sizeof(double))) != OMC_OK) return s;
+  if ((s = j->ensrc.ensure(sizeof(double))) != OMC_OK) return s;
+  if ((s = j->bl_first.ensure(first.size() * sizeof(long long))) != OMC_OK) return s;
+  if ((s = j->density.ensure(nvox * sizeof(double))) != OMC_OK) return s;
+  if ((s = j->bounds.ensure(nb * sizeof(double))) != OMC_OK) return s;
+  std::vector<double> b(nb);
+  std::copy(ph->xbounds, ph->xbounds + ph->nx + 1, b.begin());
+  std::copy(ph->ybounds, ph->ybounds + ph->ny + 1, b.begin() + ph->nx + 1);
+  std::copy(ph->zbounds, ph->zbounds + ph->nz + 1, b.begin() + ph->nx + 1 + ph->ny + 1);
+  CUDA_TRY(cudaMemcpy(j->bl_first.p, first.data(), first.size() * sizeof(long long), cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(j->density.p, ph->density, nvox * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(j->bounds.p, b.data(), nb * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemset(j->tally.p, 0, static_cast<size_t>(j->nbl) * j->nreg * sizeof(double)));
+  CUDA_TRY(cudaMemset(j->ensrc.p, 0, sizeof(double)));
+  *out = j.release();
+  return OMC_OK;
+}
+
+extern "C" omc_status omc_engine_job_dij(omc_engine *e, omc_job *j, double rel_threshold, int fp32_values,
+                                         omc_dij **out) {
+  if (!e || !j || !out) return fail(OMC_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (j->nbl < 1) return fail(OMC_ERR_ARG, "not a beamlet job");
+  if (!(rel_threshold >= 0.0)) return fail(OMC_ERR_ARG, "relative dose threshold must be >= 0");
+  if (j->done < j->nhist) return fail(OMC_ERR_STATE, "job has %lld of %lld histories left", j->nhist - j->done, j->nhist);
+  omc_status s;
+  if ((s = ensure_device(e)) != OMC_OK) return s;
+  auto *d = static_cast<omc_dij *>(std::calloc(1, sizeof(omc_dij)));
+  if (!d) return fail(OMC_ERR_NOMEM, "host allocation failed");
+  d->nrows = static_cast<int>(j->nreg - 1);
+  d->ncols = j->nbl;
+  d->col_ptr = static_cast<long long *>(std::calloc(static_cast<size_t>(j->nbl) + 1, sizeof(long long)));
+  if (!d->col_ptr) {
+    omc_dij_free(d);
+    return fail(OMC_ERR_NOMEM, "host allocation failed");
+  }
+  const double *xb = static_cast<const double *>(j->bounds.p);
+  const double *yb = xb + j->nx + 1, *zb = yb + j->ny + 1;
+  long long host_cap = 0;
+  // Tallies in groups of at most 65535 beamlets (grid y of the kernels).
+  for (int g0 = 0; g0 < j->nbl; g0 += 65535) {
+    const int ng = std::min(65535, j->nbl - g0);
+    s = dij_group_to_csc(e, static_cast<double *>(j->tally.p) + static_cast<size_t>(g0) * j->nreg, ng, j->nreg,
+                         j->nx, j->ny, xb, yb, zb, static_cast<const double *>(j->density.p), j->nh.data() + g0,
+                         j->nbatch, rel_threshold, fp32_values != 0, d, g0, host_cap);
+    if (s != OMC_OK) {
+      omc_dij_free(d);
+      return s;
+    }
+  }
+  *out = d;
   return OMC_OK;
 }
 

@@ -491,8 +491,19 @@ struct Lane {
     if constexpr (MULTI) {
       js = P.jobs + slot;
       const long long hj = js->h0 + (h - __ldg(P.slot_first + slot));
-      batch = static_cast<int>(hj / js->nperbatch);
-      init_point_history();
+      if (js->nbl > 0) {
+        int lo = 0, hi = js->nbl - 1;
+        while (lo < hi) {  // last beamlet whose first history is <= hj
+          int mid = (lo + hi + 1) >> 1;
+          if (__ldg(js->bl_first + mid) <= hj) lo = mid;
+          else hi = mid - 1;
+        }
+        batch = lo;
+        init_beamlet_history(lo);
+      } else {
+        batch = static_cast<int>(hj / js->nperbatch);
+        init_point_history();
+      }
     } else {
       if (P.S.beamlets) init_beamlet_history(__ldg(P.slot_beamlet + slot));
       else init_point_history();

@@ -3,12 +3,13 @@
 // Two threads share one engine (tables resident once):
 //  - admission: takes queued jobs in arrival order, maps their media onto
 //    the server's media, builds their regions (initRegions semantics) and
-//    uploads them (omc_engine_job_add) while rounds run on the engine's
-//    compute stream, as far as the device-memory budget and the job limit
-//    allow;
-//  - scheduler: runs rounds over the resident jobs (omc_engine_job_round,
-//    one launch), reads back and frees the jobs that finished, and wakes
-//    their waiters and the admission thread.
+//    uploads them (omc_engine_job_add, or omc_engine_job_add_dij for
+//    beamlet jobs) while rounds run on the engine's compute stream, as far
+//    as the device-memory budget and the job limit allow;
+//  - scheduler: runs rounds over the resident jobs, field and beamlet
+//    jobs together (omc_engine_job_round, one launch), reads back and frees
+//    the jobs that finished (a beamlet job as its CSC dij), and wakes their
+//    waiters and the admission thread.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -52,7 +53,7 @@ struct Job {
   double submit_s = 0, admit_s = 0, finish_s = 0;
   int rounds = 0;
   omc_status status = OMC_OK;
-  // beamlet (dij) jobs: run whole, in a turn of their own
+  // beamlet (dij) jobs: resident like field jobs, converted to CSC when done
   bool dij = false;
   int nbeams = 0;
   std::vector<int> ibeam;
@@ -119,49 +120,19 @@ omc_status job_geometry(omc_server *s, const Job &j, JobGeometry &g) {
   return omc_regions_build(g.in, g.ph, s->tab, &g.reg);
 }
 
-// Field jobs go onto the device at admission; beamlet jobs stay on the
-// host until their turn.
+// A job goes onto the device at admission: phantom, source, tallies (and
+// beamlets).
 omc_status upload_job(omc_server *s, Job &j) {
-  if (j.dij) return OMC_OK;
   JobGeometry g;
   omc_status st = job_geometry(s, j, g);
   if (st != OMC_OK) return st;
-  return omc_engine_job_add(s->eng, g.ph, g.reg, &j.src, j.nperbatch, j.nbatch, s->cfg.precision, &j.dev);
-}
-
-// A beamlet job, whole, on the server's tables (omc_engine_run_dij).  Its
-// RANMAR streams start far from the server's own and from every other
-// beamlet job's.
-omc_status run_dij_job(omc_server *s, Job &j) {
-  JobGeometry g;
-  omc_status st = job_geometry(s, j, g);
-  if (st != OMC_OK) return st;
-  if ((st = omc_engine_set_geometry(s->eng, g.ph, g.reg)) != OMC_OK) return st;
-  if ((st = omc_engine_set_source(s->eng, &j.src)) != OMC_OK) return st;
+  if (!j.dij)
+    return omc_engine_job_add(s->eng, g.ph, g.reg, &j.src, j.nperbatch, j.nbatch, s->cfg.precision, &j.dev);
   omc_beamlets b{static_cast<int>(j.ibeam.size()), j.nbeams, j.ibeam.data(), j.bl[0].data(), j.bl[1].data(),
                  j.bl[2].data(), j.bl[3].data(), j.bl[4].data(), j.bl[5].data(), j.bl[6].data(), j.bl[7].data(),
                  j.bl[8].data(), j.bl[9].data(), j.bl[10].data(), j.bl[11].data()};
-  if ((st = omc_engine_set_beamlets(s->eng, &b)) != OMC_OK) return st;
-  omc_run_config rc;
-  std::memset(&rc, 0, sizeof rc);
-  rc.nperbatch = 1;
-  rc.nbatch = j.nbatch;
-  omc_stream_seeds(s->cfg.ixx, s->cfg.jxx, (j.id % 512 + 1) << 20, &rc.ixx, &rc.jxx);
-  rc.nsplit = s->cfg.nsplit;
-  rc.precision = s->cfg.precision;
-  omc_dij_config dc;
-  std::memset(&dc, 0, sizeof dc);
-  dc.rel_threshold = j.rel_threshold;
-  dc.nhist = j.nhist.data();
-  dc.fp32_values = j.fp32_values;
-  omc_run_stats rs{};
-  st = omc_engine_run_dij(s->eng, &rc, &dc, &j.dij_out, &rs);
-  if (st == OMC_OK) {
-    std::lock_guard<std::mutex> lk(s->mu);
-    s->st.histories += rs.histories;
-    s->st.transport_s += rs.transport_ms * 1e-3;
-  }
-  return st;
+  return omc_engine_job_add_dij(s->eng, g.ph, g.reg, &j.src, &b, j.nhist.data(), 0, j.nbatch, s->cfg.precision,
+                                &j.dev);
 }
 
 void admission_loop(omc_server *s) {
@@ -200,56 +171,16 @@ void admission_loop(omc_server *s) {
 }
 
 void scheduler_loop(omc_server *s) {
-  // Field rounds continue their streams from round to round.  After a
-  // beamlet turn (which seeds the engine's streams with its own) they are
-  // seeded again, epoch e at stream (512 + e) * 2^20 of the server's
-  // sequence, so no number is drawn twice.
+  // The lanes' RANMAR streams are seeded once and continue from round to
+  // round, so no number is drawn twice.
   bool seeded = false;
-  long long epoch = 0;
   std::unique_lock<std::mutex> lk(s->mu);
   for (;;) {
     s->cv_sched.wait(lk, [&] { return s->stop || !s->resident.empty(); });
     if (s->stop) return;
     std::vector<std::shared_ptr<Job>> all = s->resident;
     lk.unlock();
-    // A beamlet job runs whole in a turn of its own: when it has the fewest
-    // histories left (shortest remaining first) or, with equal shares, when
-    // it is the oldest resident job.
-    std::shared_ptr<Job> turn;
-    {
-      long long best = -1;
-      for (auto &j : all) {
-        long long left = j->dij ? j->total() : omc_job_histories(j->dev) - omc_job_done(j->dev);
-        if (best < 0 || left < best) {
-          best = left;
-          turn = j;
-        }
-      }
-      if (s->cfg.policy == OMC_SERVE_EQUAL_SHARES) turn = all.front();
-      if (!turn->dij) turn = nullptr;
-    }
-    if (turn) {
-      omc_status st = run_dij_job(s, *turn);
-      lk.lock();
-      turn->rounds = 1;
-      turn->status = st;
-      turn->finish_s = s->now();
-      turn->state = st == OMC_OK ? JobState::Done : JobState::Failed;
-      s->resident.erase(std::remove(s->resident.begin(), s->resident.end(), turn), s->resident.end());
-      s->resident_bytes -= static_cast<long long>(turn->bytes);
-      s->st.finished++;
-      s->st.rounds++;
-      s->cv_done.notify_all();
-      s->cv_admit.notify_all();
-      if (seeded) {
-        seeded = false;
-        epoch++;
-      }
-      continue;
-    }
-    std::vector<std::shared_ptr<Job>> round;
-    for (auto &j : all)
-      if (!j->dij) round.push_back(j);
+    std::vector<std::shared_ptr<Job>> round = all;  // field and beamlet jobs alike
     const long long R = s->cfg.round_histories;
     std::vector<long long> left(round.size()), quota(round.size(), 0);
     for (size_t i = 0; i < round.size(); i++) left[i] = omc_job_histories(round[i]->dev) - omc_job_done(round[i]->dev);
@@ -300,7 +231,6 @@ void scheduler_loop(omc_server *s) {
       rc.nbatch = 1;
       rc.ixx = s->cfg.ixx;
       rc.jxx = s->cfg.jxx;
-      if (epoch) omc_stream_seeds(s->cfg.ixx, s->cfg.jxx, (512 + (epoch - 1) % 400 + 1) << 20, &rc.ixx, &rc.jxx);
       rc.nsplit = s->cfg.nsplit;
       rc.precision = s->cfg.precision;
       rc.continue_streams = seeded ? 1 : 0;
@@ -313,7 +243,9 @@ void scheduler_loop(omc_server *s) {
       j->rounds++;
       bool failed_round = st != OMC_OK;
       if (failed_round || omc_job_done(j->dev) >= omc_job_histories(j->dev)) {
-        if (!failed_round) {
+        if (!failed_round && j->dij) {
+          j->status = omc_engine_job_dij(s->eng, j->dev, j->rel_threshold, j->fp32_values, &j->dij_out);
+        } else if (!failed_round) {
           j->acc.assign(j->ph.nx * static_cast<size_t>(j->ph.ny) * j->ph.nz + 1, 0.0);
           j->acc2.assign(j->acc.size(), 0.0);
           j->status = omc_engine_job_result(s->eng, j->dev, j->acc.data(), j->acc2.data(), &j->ensrc);
@@ -454,6 +386,7 @@ extern "C" omc_status omc_server_submit_dij(omc_server *s, const omc_server_job 
   if (!s || !job || !job->phantom || !job->source || !bl || !id) return fail(OMC_ERR_ARG, "null argument");
   if (job->nbatch < 1) return fail(OMC_ERR_ARG, "need nbatch >= 1");
   if (bl->nbeamlets < 1 || bl->nbeams < 1) return fail(OMC_ERR_ARG, "need at least one beamlet and one beam");
+  if (bl->nbeamlets > 4096) return fail(OMC_ERR_ARG, "at most 4096 beamlets per job");
   if (!(rel_threshold >= 0.0)) return fail(OMC_ERR_ARG, "relative dose threshold must be >= 0");
   for (int i = 0; i < bl->nbeamlets; i++)
     if (bl->ibeam[i] < 0 || bl->ibeam[i] >= bl->nbeams) return fail(OMC_ERR_ARG, "beamlet %d: bad beam", i);
@@ -475,11 +408,9 @@ extern "C" omc_status omc_server_submit_dij(omc_server *s, const omc_server_job 
     j->nhist[i] = nhist ? nhist[i] : job->nperbatch * static_cast<long long>(job->nbatch);
   j->rel_threshold = rel_threshold;
   j->fp32_values = fp32_values;
-  // Device footprint while it runs: the beamlet tallies (bounded by the
-  // budget, which omc_engine_run_dij splits into groups) and the phantom.
-  size_t nreg = static_cast<size_t>(job->phantom->nx) * job->phantom->ny * job->phantom->nz + 1;
-  size_t tally = static_cast<size_t>(bl->nbeamlets) * nreg * sizeof(double);
-  j->bytes = std::min<size_t>(tally, static_cast<size_t>(s->cfg.hbm_budget)) + nreg * 24;
+  // Device footprint while resident: phantom, source, beamlets and one
+  // tally per beamlet.
+  j->bytes = omc_job_dij_device_bytes(job->phantom, bl->nbeamlets, s->cfg.precision);
   enqueue(s, j, id);
   return OMC_OK;
 }

@@ -43,6 +43,8 @@ def lib():
         L.omc_oracle_run.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_longlong,
                                      C.c_int, C.c_int, C.c_int, C.c_int, dp, dp, C.POINTER(Result)]
         L.omc_oracle_run.restype = C.c_int
+        L.omc_oracle_batch_totals.argtypes = [dp, C.c_int]
+        L.omc_oracle_batch_totals.restype = C.c_int
         L.omc_oracle_ranmar.argtypes = [C.c_int, C.c_int, C.c_longlong, C.POINTER(C.c_int)]
         L.omc_oracle_ranmar.restype = None
         from ompmc_gb300._native import Beamlets_t, Dij_t
@@ -75,6 +77,13 @@ def run(problem, nperbatch=None, nbatch=None, seeds=None, nsplit=None, nthreads=
     if st != 0:
         raise RuntimeError(f"oracle run failed with status {st}")
     return a, a2, res
+
+
+def batch_totals():
+    """Energy deposited inside the phantom by each batch of the last run."""
+    out = np.zeros(65536)
+    n = lib().omc_oracle_batch_totals(out.ctypes.data_as(C.POINTER(C.c_double)), len(out))
+    return out[:n].copy()
 
 
 def _beamlets_struct(b):

@@ -1793,6 +1793,18 @@ static void shower(track_t *tk) {
     }
 }
 
+/* Energy deposited inside the phantom (regions >= 1) by each batch of the
+ * last omc_oracle_run, for the batch uncertainty of the total. */
+#define ORACLE_MAX_BATCHES 65536
+static double g_batch_etot[ORACLE_MAX_BATCHES];
+static int g_batch_n;
+
+int omc_oracle_batch_totals(double *out, int cap) {
+    int n = g_batch_n < cap ? g_batch_n : cap;
+    for (int i = 0; i < n; i++) out[i] = g_batch_etot[i];
+    return n;
+}
+
 int omc_oracle_run(const omc_tables *t, const omc_phantom *ph, const omc_regions *rg, const omc_source *src,
                    int nsplit, long long nperbatch, int nbatch, int ixx, int jxx, int nthreads, double *accum_endep,
                    double *accum_endep2, omc_oracle_result *res) {
@@ -1835,13 +1847,17 @@ int omc_oracle_run(const omc_tables *t, const omc_phantom *ph, const omc_regions
                 shower(tks[0]);
             }
         }
+        double etot = 0.0;
         for (int r = 0; r < nreg; r++) {
             double e = endep[r];
             accum_endep[r] += e;
             accum_endep2[r] += e * e;
+            if (r > 0) etot += e;
         }
+        if (ib < ORACLE_MAX_BATCHES) g_batch_etot[ib] = etot;
         memset(endep, 0, nreg * sizeof(double));
     }
+    g_batch_n = nbatch < ORACLE_MAX_BATCHES ? nbatch : ORACLE_MAX_BATCHES;
     double ens = 0.0;
     for (int i = 0; i < nthreads; i++) {
         ens += tks[i]->ensrc;

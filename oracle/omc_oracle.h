@@ -46,6 +46,10 @@ int omc_oracle_run(const omc_tables *t, const omc_phantom *ph,
                    int nthreads, double *accum_endep, double *accum_endep2,
                    omc_oracle_result *res);
 
+/* Energy deposited inside the phantom by each batch of the last
+ * omc_oracle_run (at most cap values); returns how many were written. */
+int omc_oracle_batch_totals(double *out, int cap);
+
 /* The omc_matrad beamlet loop (ucodes/omc_matrad/omc_matrad.c:1374-1512):
  * beamlet by beamlet, nbatch batches of (nhist[ib] or nperbatch*nbatch)/
  * nbatch histories from the beamlet source (initHistory(ibeamlet),

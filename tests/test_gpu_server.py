@@ -148,11 +148,12 @@ def column_sums(col, vals):
 
 
 def test_beamlet_jobs_beside_field_jobs(engine, problem_factory, tmp_path):
-    """Beamlet jobs queued among a field job: each gives the dij that
-    omc_engine_run_dij gives (per-beamlet integral doses over 16 jobs
-    against 16 engine runs on disjoint streams, within their spread), and
-    the field job, whose rounds are cut by the beamlet turns, gives the dose
-    omc_engine_run gives."""
+    """Beamlet jobs queued among a field job share its rounds (launches):
+    each gives the dij that omc_engine_run_dij gives for the beamlets alone
+    (per-beamlet integral doses over 16 jobs against 16 engine runs on
+    disjoint streams, within their spread; the same CSC shape), and the
+    field job, whose rounds carried the beamlet jobs' histories, gives the
+    dose omc_engine_run gives."""
     from cases import dij_case, run_seeds
 
     inp, _, bl, _, _, _ = dij_case("dij_slab", str(tmp_path / "d"), ncase=1000, nbatch=2)
@@ -176,11 +177,13 @@ def test_beamlet_jobs_beside_field_jobs(engine, problem_factory, tmp_path):
     finally:
         srv.close()
     for col, rows, vals, r in outs:
-        assert r.status == 0 and r.rounds == 1
+        assert r.status == 0 and r.rounds >= 1
         assert r.histories == bl.n * 2000
         assert len(col) == bl.n + 1 and col[-1] == len(rows) == len(vals)
+        assert np.all(np.diff(col) > 0) and rows.max() < prob.nreg - 1
     assert fr.rounds > 10 and st.finished == k + 1
-    assert fr.finish_s > max(o[3].finish_s for o in outs)  # beamlet turns came between its rounds
+    assert st.max_round_jobs >= 2  # beamlet and field histories in one launch
+    assert fr.finish_s > min(o[3].finish_s for o in outs)  # beamlet jobs finished while the field job ran
     srv_sums = np.stack([column_sums(o[0], o[2]) for o in outs])
     engine.load(prob)
     engine.set_beamlets(bl)
