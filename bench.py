@@ -274,11 +274,13 @@ def fp32_dose_error(a32, b32, H32, K32, roi32, tot32, a64, b64, H64, K64, roi64,
     v32 = np.maximum(b32[1:] / K32 / H32 ** 2 - m32 ** 2, 0) / (K32 - 1)
     v64 = np.maximum(b64[1:] / K64 / H64 ** 2 - m64 ** 2, 0) / (K64 - 1)
     va, vb = v32[sel20], v64[sel20]
+    ok = (va + vb) > 0
+    va, vb = va[ok], vb[ok]
     sig = np.sqrt(va + vb)
-    t = (m32[sel20] - m64[sel20]) / np.where(sig > 0, sig, np.inf)
+    t = (m32[sel20][ok] - m64[sel20][ok]) / sig
     # Welch-Satterthwaite degrees of freedom per voxel: the two runs have
     # different history counts, so their batch variances differ.
-    dof = (va + vb) ** 2 / np.maximum(va ** 2 / (K32 - 1) + vb ** 2 / (K64 - 1), 1e-300)
+    dof = (va + vb) ** 2 / (va ** 2 / (K32 - 1) + vb ** 2 / (K64 - 1))
     z = S.norm.ppf(np.clip(S.t.cdf(t, dof), 1e-300, 1 - 1e-16))
     roi_d, roi_s = batch_ratio(np.asarray(roi32) / H32, np.asarray(roi64) / H64)
     tot_d, tot_s = batch_ratio(np.asarray(tot32) / H32, np.asarray(tot64) / H64)

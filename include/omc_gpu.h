@@ -261,6 +261,11 @@ typedef struct omc_run_config {
                             interactions run inline and a take follows an
                             electron to the end of its track; 0 = auto,
                             -1 = never                                    */
+    int history_stats;   /* wavefront: 1 = also score the history-by-history
+                            sums of x and x^2 per region (x = energy one
+                            history deposits there), read back with
+                            omc_engine_history_sums; 0 = batch sums only
+                            (the reference's method)                      */
 } omc_run_config;
 
 typedef enum omc_schedule {
@@ -325,6 +330,21 @@ omc_status omc_engine_run_resident(omc_engine *e, const omc_run_config *cfg,
                                    const double **d_accum_endep,
                                    const double **d_accum_endep2,
                                    omc_run_stats *stats);
+
+/* History-by-history sums of the last run made with
+ * cfg->history_stats = 1 (nreg entries each, may be NULL): sum[r] and
+ * sum2[r] over histories of x and x^2, x the energy (MeV) one history
+ * deposited in region r, the estimators of Walters, Kawrakow and Rogers,
+ * Med. Phys. 29 (2002) 2745: mean = sum/N, variance of the mean =
+ * (sum2/N - mean^2)/(N - 1).  *histories = histories merged (N when no
+ * error flag is set); *split = histories that touched more regions than
+ * the merge table holds (they count as several histories; zero in
+ * practice).  The reference has only the batch method (accumEndep,
+ * omc_dosxyz.c:696-755), which every run still returns.  History tracking
+ * needs a pool of about 1.5 * inflight blocks of 384 bytes on the device
+ * during the run; OMC_ERR_STATE if the last run did not track histories. */
+omc_status omc_engine_history_sums(omc_engine *e, double *sum, double *sum2,
+                                   long long *histories, long long *split);
 
 /* Weighted sums of the batch tallies of the last run: out[b] = sum over
  * regions r of weights[r] * (energy batch b deposited in r), for the

@@ -63,7 +63,7 @@ class RunConfig_t(C.Structure):
                 ("nsplit", C.c_int), ("precision", C.c_int), ("nlanes", C.c_int),
                 ("stack_depth", C.c_int), ("serial", C.c_int), ("continue_streams", C.c_int),
                 ("schedule", C.c_int), ("inflight", C.c_longlong), ("chunk_events", C.c_int),
-                ("drain_per_warp", C.c_int)]
+                ("drain_per_warp", C.c_int), ("history_stats", C.c_int)]
 
 
 class RunStats_t(C.Structure):
@@ -170,6 +170,8 @@ def lib(path: str | None = None):
         "omc_engine_set_source": ([vp, pp(Source_t)], C.c_int),
         "omc_engine_run": ([vp, pp(RunConfig_t), pp(C.c_double), pp(C.c_double), pp(RunStats_t)], C.c_int),
         "omc_engine_run_resident": ([vp, pp(RunConfig_t), pp(vp), pp(vp), pp(RunStats_t)], C.c_int),
+        "omc_engine_history_sums": ([vp, pp(C.c_double), pp(C.c_double), pp(C.c_longlong), pp(C.c_longlong)],
+                                    C.c_int),
         "omc_engine_batch_sums": ([vp, pp(C.c_double), pp(C.c_double), pp(C.c_int)], C.c_int),
         "omc_engine_run_noalloc": ([vp, pp(RunConfig_t), C.c_void_p, C.c_void_p, pp(RunStats_t)], C.c_int),
         "omc_engine_set_beamlets": ([vp, pp(Beamlets_t)], C.c_int),

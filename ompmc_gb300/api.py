@@ -207,19 +207,20 @@ class Engine:
 
     @staticmethod
     def config(nperbatch, nbatch, seeds=(97, 33), nsplit=1, precision=FP64, nlanes=0, stack_depth=0, serial=0,
-               continue_streams=0, schedule=AUTO, inflight=0, chunk_events=0, drain_per_warp=0):
+               continue_streams=0, schedule=AUTO, inflight=0, chunk_events=0, drain_per_warp=0, history_stats=0):
         return N.RunConfig_t(int(nperbatch), int(nbatch), int(seeds[0]), int(seeds[1]), int(nsplit),
                              int(precision), int(nlanes), int(stack_depth), int(serial), int(continue_streams),
-                             int(schedule), int(inflight), int(chunk_events), int(drain_per_warp))
+                             int(schedule), int(inflight), int(chunk_events), int(drain_per_warp),
+                             int(history_stats))
 
     def run(self, nperbatch=None, nbatch=None, seeds=None, nsplit=None, precision=FP64, nlanes=0,
             stack_depth=0, serial=0, continue_streams=0, schedule=AUTO, inflight=0, chunk_events=0,
-            drain_per_warp=0):
+            drain_per_warp=0, history_stats=0):
         p = self._problem
         cfg = self.config(p.nperbatch if nperbatch is None else nperbatch, p.nbatch if nbatch is None else nbatch,
                           p.seeds if seeds is None else seeds, p.nsplit if nsplit is None else nsplit,
                           precision, nlanes, stack_depth, serial, continue_streams, schedule, inflight,
-                          chunk_events, drain_per_warp)
+                          chunk_events, drain_per_warp, history_stats)
         a = np.zeros(p.nreg)
         a2 = np.zeros(p.nreg)
         st = N.RunStats_t()
@@ -231,6 +232,15 @@ class Engine:
         st = N.RunStats_t()
         check(N.lib().omc_engine_run_resident(self._h, C.byref(cfg), C.byref(d1), C.byref(d2), C.byref(st)))
         return d1.value, d2.value, st
+
+    def history_sums(self):
+        """(sum, sum2, histories, split) of the last run made with
+        history_stats=1 (omc_engine_history_sums)."""
+        n = self._problem.nreg
+        a, a2 = np.zeros(n), np.zeros(n)
+        h, sp = C.c_longlong(), C.c_longlong()
+        check(N.lib().omc_engine_history_sums(self._h, _dptr(a), _dptr(a2), C.byref(h), C.byref(sp)))
+        return a, a2, h.value, sp.value
 
     def batch_sums(self, weights):
         """Per-batch weighted sums of the last run's batch tallies

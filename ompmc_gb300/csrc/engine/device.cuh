@@ -28,7 +28,9 @@ enum : unsigned {
   ERR_EVENTS = 4u,     // a history exceeded the event cap: history dropped
   ERR_TABLE = 8u,      // an interpolation index left its table (clamped)
   ERR_QUEUE = 16u,     // wavefront queue full: particle dropped
-  ERR_BARRIER = 32u    // a grid barrier gave up waiting
+  ERR_BARRIER = 32u,   // a grid barrier gave up waiting
+  ERR_HISTORY = 64u    // history-by-history scoring: block pool empty or a
+                       // history over its region limit (its sums are split)
 };
 
 // Iteration caps of device loops.  The reference's loops end with
@@ -174,6 +176,44 @@ struct JobSlot {
 // beamlet).
 constexpr int kBatchTag = 4096;
 
+// History-by-history scoring (wavefront schedule, optional).  Every
+// history in flight owns a chain of blocks from a pool; its particles carry
+// the head block in their queue tag, each deposit appends (region, energy)
+// to the chain, and the head block counts the history's particles in flight.
+// The lane whose take brings that count to zero merges the chain by region
+// and adds the history's energy x in each region to sum[r] and x^2 to
+// sum2[r] -- the history-by-history estimators of Walters, Kawrakow and
+// Rogers (Med. Phys. 29 (2002) 2745) -- then returns the blocks.  Blocks
+// of 384 bytes: a 16-byte header and (region, energy) entries.
+constexpr int kHbhBlockBytes = 384;
+constexpr int kHbhRegions = 128;  // distinct regions a history merges at once (local table)
+template <typename R>
+struct HbhBlock {
+  static constexpr int kEntries = (kHbhBlockBytes - 16) / static_cast<int>(4 + sizeof(R));
+  int count;  // entries appended; those past kEntries went to the next block
+  int next;   // continuation block, -1 none
+  int live;   // head block: particles of the history queued or being processed
+  int slot;   // head block: tally slot (batch) of the history
+  int ir[kEntries];
+  R x[kEntries];
+};
+
+// Free blocks: two rings of block ids, each with pop and push counters.
+// In wavefront iteration it, blocks are returned to ring it & 1 and taken
+// from the other ring, so no ring is pushed and popped at once and a pop
+// never reads an entry that a push is still writing.
+template <typename R>
+struct HbhPool {
+  HbhBlock<R> *blocks;
+  int nblocks;
+  int *ring;                  // [2][nblocks]
+  unsigned long long *pop;    // [2] ids taken from each ring
+  unsigned long long *push;   // [2] ids returned to each ring
+  double *sum, *sum2;         // [nreg] sums over histories of x and x^2
+  unsigned long long *histories;  // histories merged
+  unsigned long long *split;      // histories merged in parts (over the local region table)
+};
+
 template <typename R>
 struct Params {
   Tables<R> T;
@@ -205,6 +245,7 @@ struct Params {
   unsigned long long *n_dep;
   int *max_np;
   unsigned *err;
+  HbhPool<R> hbh;            // history-by-history scoring (blocks null: off)
 };
 
 // ---------------------------------------------------------------------------

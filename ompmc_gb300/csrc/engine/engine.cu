@@ -180,6 +180,11 @@ struct Wavefront {
   int trace_cap;              // iterations the trace holds
   int chunk_events;           // electron steps per take before re-queueing
   unsigned long long drain_below;  // drain mode below this many particles in flight
+  // history-by-history scoring: free blocks of the next iteration's pop
+  // ring (a lower bound, [2] by iteration parity) and the blocks an
+  // iteration keeps back for continuation blocks
+  unsigned long long *hbh_free;
+  unsigned long long hbh_reserve;
 };
 
 constexpr int kDefaultChunkEvents = 1;
@@ -234,7 +239,7 @@ __device__ bool grid_barrier(unsigned *arrive, unsigned *gen, unsigned nblocks) 
 
 __device__ __forceinline__ unsigned vload(const unsigned *p) { return *static_cast<const volatile unsigned *>(p); }
 
-template <typename R, bool MULTI>
+template <typename R, bool MULTI, bool HBH = false>
 __global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) wavefront_kernel(Params<R> P, Wavefront<R> W) {
   extern __shared__ unsigned char s_raw[];
   const int t = threadIdx.x;
@@ -242,7 +247,7 @@ __global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) wavefront_ke
   const int lane_id = t & 31;
   RngPlanes sp = rng_planes(s_raw);
   rng_to_smem(P.rng_u, P.nlanes, gtid, sp, t);
-  Lane<R, true, MULTI> L(P, gtid, sp.lo + t, sp.hi + t, kBlock);
+  Lane<R, true, MULTI, HBH> L(P, gtid, sp.lo + t, sp.hi + t, kBlock);
   L.rng.i = P.rng_ijc[gtid];
   L.rng.j = P.rng_ijc[P.nlanes + gtid];
   L.rng.c = P.rng_ijc[2 * P.nlanes + gtid];
@@ -279,6 +284,17 @@ __global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) wavefront_ke
     long long m = static_cast<long long>(W.target) - static_cast<long long>(inflight);
     if (m < 0) m = 0;
     if (m > remaining) m = remaining;
+    if constexpr (HBH) {
+      // Blocks are returned to ring it & 1 and taken from the other one,
+      // whose push count does not move during this iteration.  A new
+      // history needs a head block; some are kept for continuations.
+      L.hbh_push_ring = it & 1;
+      L.hbh_pop_ring = bout;
+      L.hbh_pop_limit = *static_cast<volatile unsigned long long *>(P.hbh.push + bout);
+      const long long nfree = static_cast<long long>(*static_cast<volatile unsigned long long *>(W.hbh_free + bin)) -
+                              static_cast<long long>(W.hbh_reserve);
+      if (m > nfree) m = nfree > 0 ? nfree : 0;
+    }
     if (gtid == 0) {
       W.ctr[cfree] = 0;
       W.ctr[3 + cfree] = 0;
@@ -316,7 +332,9 @@ __global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) wavefront_ke
         const unsigned long long k = i - r_in;
         if (k < static_cast<unsigned long long>(m)) {
           L.init_history(static_cast<long long>(injected + k));
+          if constexpr (HBH) L.hbh_start();
           L.emit(L.p);
+          if constexpr (HBH) L.hbh_finish(0);
         }
       } else if (base >= r_ph && base < r_ph + ph_pad) {
         const unsigned long long k = i - r_ph;
@@ -324,6 +342,7 @@ __global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) wavefront_ke
           L.take(W.ph_f[bin], W.ph_k[bin], static_cast<unsigned>(k), W.ph_s[bin]);
           L.wf_photon_event();
           events++;
+          if constexpr (HBH) L.hbh_finish(1);
         }
       } else if (base >= r_pi && base < r_pi + pi_pad) {
         const unsigned long long k = i - r_pi;
@@ -332,6 +351,7 @@ __global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) wavefront_ke
           const bool survivor = L.p.iq == 2;
           L.p.iq = 0;
           L.deferred_photon_interaction(survivor);
+          if constexpr (HBH) L.hbh_finish(1);
         }
       } else if (base >= r_el && base < r_el + el_pad) {
         const unsigned long long k = i - r_el;
@@ -357,6 +377,7 @@ __global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) wavefront_ke
             if (L.pending_interaction) L.emit_pending();
             else L.emit(L.p);
           }
+          if constexpr (HBH) L.hbh_finish(1);
         }
       } else {
         const unsigned long long k = i - r_ei;
@@ -364,7 +385,18 @@ __global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) wavefront_ke
           L.take(W.ei_f[bin], W.ei_k[bin], static_cast<unsigned>(k), W.ei_s[bin]);
           L.deferred_interaction();
           if (L.alive) L.emit(L.p);
+          if constexpr (HBH) L.hbh_finish(1);
         }
+      }
+    }
+    if constexpr (HBH) {
+      // Free blocks of the next iteration's pop ring (the ring this one
+      // fills): its pops are final, its pushes can only grow after this
+      // read, so the difference is a lower bound for every thread.
+      if (gtid == 0) {
+        const int nr = it & 1;
+        W.hbh_free[bout] = *static_cast<volatile unsigned long long *>(P.hbh.push + nr) -
+                           *static_cast<volatile unsigned long long *>(P.hbh.pop + nr);
       }
     }
     if (!grid_barrier(W.bar_arrive, W.bar_gen, gridDim.x)) L.err |= ERR_BARRIER;
@@ -379,6 +411,10 @@ __global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) wavefront_ke
   atomicAdd(P.n_geom, L.n_geom);
   atomicAdd(P.n_dep, L.n_dep);
   atomicMax(W.hwm, L.queue_hwm);
+  if constexpr (HBH) {
+    if (L.hbh_merged) atomicAdd(P.hbh.histories, L.hbh_merged);
+    if (L.hbh_split) atomicAdd(P.hbh.split, L.hbh_split);
+  }
   if (gtid == 0) *W.iters = it;
   if (L.err) atomicOr(P.err, L.err);
 }
@@ -676,6 +712,10 @@ struct omc_engine {
   DevBuf batch_tally, batch_first;
   int batch_tallies = 0;  // batches whose tallies the last run left in batch_tally (0: none)
   DevBuf weights, batch_dot;
+  // history-by-history scoring: block pool, rings, counters, sums
+  DevBuf hbh_blocks, hbh_ring, hbh_ctr, hbh_sum, hbh_sum2;
+  bool hbh_valid = false;  // the last run tracked histories
+  long long hbh_histories = 0, hbh_split = 0;
   // per-iteration trace of the last wavefront launch (diagnostics)
   DevBuf trace;
   int trace_cap = 0;
@@ -1019,14 +1059,35 @@ struct WfCounters {
   unsigned hwm;
 };
 
-template <typename R, bool MULTI = false>
+template <typename R, bool MULTI = false, bool HBH = false>
 int wavefront_blocks(omc_engine *e) {
   size_t smem = kRngSmem;
-  cudaFuncSetAttribute(wavefront_kernel<R, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaFuncSetAttribute(wavefront_kernel<R, MULTI, HBH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        static_cast<int>(smem));
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wavefront_kernel<R, MULTI>, kBlock, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wavefront_kernel<R, MULTI, HBH>, kBlock, smem);
   return (per_sm < 1 ? 1 : per_sm) * e->nsm;
+}
+
+// Counters of the history-by-history pool (one device buffer).
+struct HbhCounters {
+  unsigned long long pop[2], push[2];
+  unsigned long long free[2];  // Wavefront::hbh_free
+  unsigned long long histories, split;
+};
+
+// A full pool: every block id in ring 1, which iteration 0 pops.
+__global__ void hbh_init_kernel(int *ring, int nblocks, HbhCounters *c) {
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < nblocks;
+       i += static_cast<long long>(gridDim.x) * blockDim.x)
+    ring[nblocks + i] = static_cast<int>(i);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    c->pop[0] = c->pop[1] = 0;
+    c->push[0] = 0;
+    c->push[1] = static_cast<unsigned long long>(nblocks);
+    c->free[0] = static_cast<unsigned long long>(nblocks);
+    c->free[1] = 0;
+  }
 }
 
 template <typename R>
@@ -1043,7 +1104,8 @@ omc_status run_wavefront(omc_engine *e, PrecisionState<R> &S, const omc_run_conf
   // to two particles per split, every electron step up to two.
   unsigned long long cap = target * (4ull + 2ull * nsplit) + 4ull * nlanes;
   if (cap > 0x7fffffffull) cap = 0x7fffffffull;
-  const size_t tag_bytes = job ? static_cast<size_t>(cap) * sizeof(int) : 0;
+  const bool hbh = cfg->history_stats != 0 && !(job && job->jobs);
+  const size_t tag_bytes = (job || hbh) ? static_cast<size_t>(cap) * sizeof(int) : 0;
   size_t per_queue = static_cast<size_t>(cap) * (8 * sizeof(R) + sizeof(int)) + tag_bytes;
   const int nqueues = 8;  // photons, electrons, electron and photon interactions; two generations each
   if (S.queue.ensure(nqueues * per_queue) != OMC_OK) return OMC_ERR_NOMEM;
@@ -1053,7 +1115,7 @@ omc_status run_wavefront(omc_engine *e, PrecisionState<R> &S, const omc_run_conf
   for (int q = 0; q < nqueues; q++) {
     R *f = reinterpret_cast<R *>(qb + q * per_queue);
     int *k = reinterpret_cast<int *>(qb + q * per_queue + static_cast<size_t>(cap) * 8 * sizeof(R));
-    int *tag = job ? k + cap : nullptr;
+    int *tag = (job || hbh) ? k + cap : nullptr;
     if (q < 2) {
       W.ph_f[q] = f;
       W.ph_k[q] = k;
@@ -1110,6 +1172,31 @@ omc_status run_wavefront(omc_engine *e, PrecisionState<R> &S, const omc_run_conf
   P.max_np = &dc->max_np;
   P.err = &dc->err;
   apply_job(P, S, job, e->nreg);
+  // History-by-history pool: a head block per history in flight plus
+  // continuation blocks; an iteration keeps 4 blocks per thread back for
+  // continuations.
+  HbhCounters *hc_dev = nullptr;
+  int hbh_nblocks = 0;
+  if (hbh) {
+    const unsigned long long nb = target + target / 2 + 8ull * nlanes;
+    if (nb > 0x7fffffffull) return fail(OMC_ERR_ARG, "history tracking: %llu blocks exceed the pool index", nb);
+    hbh_nblocks = static_cast<int>(nb);
+    if (e->hbh_blocks.ensure(nb * sizeof(HbhBlock<R>)) != OMC_OK) return OMC_ERR_NOMEM;
+    if (e->hbh_ring.ensure(2 * nb * sizeof(int)) != OMC_OK) return OMC_ERR_NOMEM;
+    if (e->hbh_ctr.ensure(sizeof(HbhCounters)) != OMC_OK) return OMC_ERR_NOMEM;
+    hc_dev = static_cast<HbhCounters *>(e->hbh_ctr.p);
+    P.hbh.blocks = static_cast<HbhBlock<R> *>(e->hbh_blocks.p);
+    P.hbh.nblocks = hbh_nblocks;
+    P.hbh.ring = static_cast<int *>(e->hbh_ring.p);
+    P.hbh.pop = hc_dev->pop;
+    P.hbh.push = hc_dev->push;
+    P.hbh.sum = static_cast<double *>(e->hbh_sum.p);
+    P.hbh.sum2 = static_cast<double *>(e->hbh_sum2.p);
+    P.hbh.histories = &hc_dev->histories;
+    P.hbh.split = &hc_dev->split;
+    W.hbh_free = hc_dev->free;
+    W.hbh_reserve = 4ull * nlanes;
+  }
   const int nlaunch = job ? 1 : cfg->nbatch;
   size_t smem = kRngSmem;
   cudaEvent_t t0, t1;
@@ -1120,8 +1207,13 @@ omc_status run_wavefront(omc_engine *e, PrecisionState<R> &S, const omc_run_conf
   cudaError_t err = cudaSuccess;
   for (int b = 0; b < nlaunch && err == cudaSuccess; b++) {
     cudaMemsetAsync(wc, 0, sizeof(WfCounters), e->stream);
+    if (hbh) {
+      hbh_init_kernel<<<std::max(1, std::min(4 * e->nsm, (hbh_nblocks + 255) / 256)), 256, 0, e->stream>>>(
+          P.hbh.ring, hbh_nblocks, hc_dev);
+    }
     void *args[] = {&P, &W};
     void *fn = (job && job->jobs) ? reinterpret_cast<void *>(wavefront_kernel<R, true>)
+               : hbh              ? reinterpret_cast<void *>(wavefront_kernel<R, false, true>)
                                   : reinterpret_cast<void *>(wavefront_kernel<R, false>);
     err = cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(kBlock), args, smem, e->stream);
     if (job) continue;
@@ -1141,6 +1233,12 @@ omc_status run_wavefront(omc_engine *e, PrecisionState<R> &S, const omc_run_conf
   WfCounters hw{};
   cudaMemcpy(&hc, dc, sizeof hc, cudaMemcpyDeviceToHost);
   cudaMemcpy(&hw, wc, sizeof hw, cudaMemcpyDeviceToHost);
+  if (hbh) {
+    HbhCounters hh{};
+    cudaMemcpy(&hh, hc_dev, sizeof hh, cudaMemcpyDeviceToHost);
+    e->hbh_histories += static_cast<long long>(hh.histories);
+    e->hbh_split += static_cast<long long>(hh.split);
+  }
   iters_total = hw.iters;
   e->trace_iters = hw.iters;
   if (stats) {
@@ -1230,7 +1328,8 @@ extern "C" void omc_engine_destroy(omc_engine *e) {
   e->f32.beamlets.clear();
   for (DevBuf *b : {&e->dij_tally, &e->dij_first, &e->dij_beamlet, &e->dij_nhist, &e->dij_max, &e->dij_cnt,
                     &e->dij_off, &e->dij_rows, &e->dij_vals, &e->multi_slots, &e->multi_first, &e->trace,
-                    &e->batch_tally, &e->batch_first, &e->dij_factor, &e->weights, &e->batch_dot})
+                    &e->batch_tally, &e->batch_first, &e->dij_factor, &e->weights, &e->batch_dot,
+                    &e->hbh_blocks, &e->hbh_ring, &e->hbh_ctr, &e->hbh_sum, &e->hbh_sum2})
     b->release();
   cudaStreamDestroy(e->stream);
   delete e;
@@ -1386,7 +1485,12 @@ static omc_status prepare_run(omc_engine *e, const omc_run_config *cfg, RunPlan 
   if ((s = ensure_device(e)) != OMC_OK) return s;
   rp.fp64 = cfg->precision == OMC_FP64;
   rp.wavefront = !cfg->serial && cfg->schedule != OMC_SCHEDULE_LANES;
-  if (rp.wavefront) rp.nlanes = (rp.fp64 ? wavefront_blocks<double>(e) : wavefront_blocks<float>(e)) * kBlock;
+  if (cfg->history_stats && !rp.wavefront)
+    return fail(OMC_ERR_ARG, "history-by-history scoring needs the wavefront schedule");
+  if (rp.wavefront && cfg->history_stats)
+    rp.nlanes = (rp.fp64 ? wavefront_blocks<double, false, true>(e) : wavefront_blocks<float, false, true>(e)) * kBlock;
+  else if (rp.wavefront)
+    rp.nlanes = (rp.fp64 ? wavefront_blocks<double>(e) : wavefront_blocks<float>(e)) * kBlock;
   else if (cfg->serial) rp.nlanes = 1;
   else rp.nlanes = cfg->nlanes > 0 ? cfg->nlanes : (rp.fp64 ? default_lanes<double>(e) : default_lanes<float>(e));
   rp.depth = cfg->stack_depth > 0 ? cfg->stack_depth : kDefaultDepth + 4 * std::max(1, cfg->nsplit);
@@ -1412,6 +1516,14 @@ static omc_status engine_run(omc_engine *e, const omc_run_config *cfg, omc_run_s
   const bool fp64 = rp.fp64, wavefront = rp.wavefront;
   const int nlanes = rp.nlanes, depth = rp.depth;
   e->batch_tallies = 0;
+  e->hbh_valid = false;
+  e->hbh_histories = e->hbh_split = 0;
+  if (cfg->history_stats) {
+    if ((s = e->hbh_sum.ensure(e->nreg * sizeof(double))) != OMC_OK) return s;
+    if ((s = e->hbh_sum2.ensure(e->nreg * sizeof(double))) != OMC_OK) return s;
+    CUDA_TRY(cudaMemsetAsync(e->hbh_sum.p, 0, e->nreg * sizeof(double), e->stream));
+    CUDA_TRY(cudaMemsetAsync(e->hbh_sum2.p, 0, e->nreg * sizeof(double), e->stream));
+  }
   cudaMemsetAsync(e->endep.p, 0, e->nreg * sizeof(double), e->stream);
   cudaMemsetAsync(e->acc.p, 0, e->nreg * sizeof(double), e->stream);
   cudaMemsetAsync(e->acc2.p, 0, e->nreg * sizeof(double), e->stream);
@@ -1429,9 +1541,23 @@ static omc_status engine_run(omc_engine *e, const omc_run_config *cfg, omc_run_s
   return fp64 ? run_batches(e, e->f64, cfg, nlanes, depth, stats) : run_batches(e, e->f32, cfg, nlanes, depth, stats);
 }
 
+extern "C" omc_status omc_engine_history_sums(omc_engine *e, double *sum, double *sum2, long long *histories,
+                                              long long *split) {
+  if (!e) return fail(OMC_ERR_ARG, "null argument");
+  if (!e->hbh_valid) return fail(OMC_ERR_STATE, "the last run did not score history by history (history_stats)");
+  omc_status s;
+  if ((s = ensure_device(e)) != OMC_OK) return s;
+  if (sum) CUDA_TRY(cudaMemcpy(sum, e->hbh_sum.p, e->nreg * sizeof(double), cudaMemcpyDeviceToHost));
+  if (sum2) CUDA_TRY(cudaMemcpy(sum2, e->hbh_sum2.p, e->nreg * sizeof(double), cudaMemcpyDeviceToHost));
+  if (histories) *histories = e->hbh_histories;
+  if (split) *split = e->hbh_split;
+  return OMC_OK;
+}
+
 extern "C" omc_status omc_engine_run(omc_engine *e, const omc_run_config *cfg, double *accum_endep,
                                      double *accum_endep2, omc_run_stats *stats) {
   omc_status s = engine_run(e, cfg, stats);
+  if (cfg && cfg->history_stats && (s == OMC_OK || s == OMC_ERR_STACK || s == OMC_ERR_LIMIT)) e->hbh_valid = true;
   if (s != OMC_OK && s != OMC_ERR_STACK && s != OMC_ERR_LIMIT) return s;
   if (accum_endep) cudaMemcpy(accum_endep, e->acc.p, e->nreg * sizeof(double), cudaMemcpyDeviceToHost);
   if (accum_endep2) cudaMemcpy(accum_endep2, e->acc2.p, e->nreg * sizeof(double), cudaMemcpyDeviceToHost);
@@ -1475,6 +1601,7 @@ extern "C" omc_status omc_engine_tune(omc_engine *e, const omc_run_config *cfg, 
 extern "C" omc_status omc_engine_run_resident(omc_engine *e, const omc_run_config *cfg, const double **d_acc,
                                               const double **d_acc2, omc_run_stats *stats) {
   omc_status s = engine_run(e, cfg, stats);
+  if (cfg && cfg->history_stats && (s == OMC_OK || s == OMC_ERR_STACK || s == OMC_ERR_LIMIT)) e->hbh_valid = true;
   if (d_acc) *d_acc = static_cast<const double *>(e->acc.p);
   if (d_acc2) *d_acc2 = static_cast<const double *>(e->acc2.p);
   return s;
@@ -1649,6 +1776,7 @@ omc_status dij_group_to_csc(omc_engine *e, double *tally, int ng, long long nreg
 
 omc_status run_dij(omc_engine *e, const omc_run_config *cfg, const omc_dij_config *dc, omc_dij *out,
                    omc_run_stats *stats) {
+  if (cfg->history_stats) return fail(OMC_ERR_ARG, "history-by-history scoring is for dose runs, not dij runs");
   RunPlan rp;
   omc_status s = prepare_run(e, cfg, rp);
   if (s != OMC_OK) return s;
@@ -1990,6 +2118,7 @@ extern "C" omc_status omc_engine_job_round(omc_engine *e, omc_job *const *jobs, 
   if (!e || !jobs || !quota || !cfg || njobs < 1) return fail(OMC_ERR_ARG, "bad argument");
   if (!e->f64.tables_ok) return fail(OMC_ERR_STATE, "omc_engine_set_tables must come first");
   if (njobs > (1 << 19)) return fail(OMC_ERR_ARG, "too many jobs in one round");
+  if (cfg->history_stats) return fail(OMC_ERR_ARG, "history-by-history scoring is for single-job runs");
   const int prec = jobs[0]->precision;
   for (int i = 0; i < njobs; i++) {
     if (!jobs[i] || jobs[i]->precision != prec) return fail(OMC_ERR_ARG, "jobs of one round share one precision");

@@ -81,7 +81,7 @@ __device__ __forceinline__ unsigned lanemask_lt() {
   return m;
 }
 
-template <typename R, bool WF, bool MULTI = false>
+template <typename R, bool WF, bool MULTI = false, bool HBH = false>
 struct Lane {
   const Params<R> &P;
   Ranmar rng;
@@ -103,6 +103,14 @@ struct Lane {
   int max_np;
   unsigned long long n_geom;  // howfar calls (voxel-stepping decisions)
   unsigned long long n_dep;   // ausgab calls (energy deposits)
+  // history-by-history scoring (HBH): head block of the current particle's
+  // history (-1: not tracked), particles emitted by the current take, the
+  // rings of this iteration and the ids the pop ring holds
+  int hblk = -1;
+  int emitted = 0;
+  int hbh_pop_ring = 1, hbh_push_ring = 0;
+  unsigned long long hbh_pop_limit = 0;
+  unsigned long long hbh_merged = 0, hbh_split = 0;
 
   __device__ Lane(const Params<R> &prm, int ln, unsigned short *slo, unsigned char *shi, int sstride)
       : P(prm), lane(ln) {
@@ -235,7 +243,12 @@ struct Lane {
     __stcg(f + 6 * c + slot, q.w);
     __stcg(f + 7 * c + slot, q.wt);
     __stcg(k + slot, q.ir * 4 + (q.iq + 1));
-    if (tag) __stcg(tag + slot, tag_value());
+    if constexpr (HBH) {
+      __stcg(tag + slot, hblk);
+      emitted++;
+    } else if (tag) {
+      __stcg(tag + slot, tag_value());
+    }
   }
   __device__ __forceinline__ void emit(const Particle<R> &q) {
     if (q.iq == 0) emit_to(out.ph_f, out.ph_k, out.ph_n, q, out.ph_s);
@@ -251,7 +264,14 @@ struct Lane {
     emit_to(out.pi_f, out.pi_k, out.pi_n, t, out.pi_s);
   }
   __device__ __forceinline__ void take(const R *f, const int *k, unsigned slot, const int *tag) {
-    if (tag) set_tag(__ldcg(tag + slot));
+    if constexpr (HBH) {
+      // The tag is the history's head block; the block holds the tally slot.
+      hblk = __ldcg(tag + slot);
+      emitted = 0;
+      if (hblk >= 0) this->slot = __ldcg(&P.hbh.blocks[hblk].slot);
+    } else if (tag) {
+      set_tag(__ldcg(tag + slot));
+    }
     size_t c = queue_cap;
     p.e = __ldcg(f + slot);
     p.x = __ldcg(f + c + slot);
@@ -274,6 +294,135 @@ struct Lane {
       atomicAdd(js->tally + static_cast<size_t>(batch) * js->nreg + ir, static_cast<double>(wt * edep));
     else
       atomicAdd(P.endep + static_cast<size_t>(slot) * P.tally_stride + ir, static_cast<double>(wt * edep));
+    if constexpr (HBH) hbh_append(ir, wt * edep);
+  }
+
+  // ---- history-by-history scoring (HBH) --------------------------------------
+  __device__ int hbh_pop() {
+    const int r = hbh_pop_ring;
+    const unsigned long long i = atomicAdd(P.hbh.pop + r, 1ull);
+    if (i >= hbh_pop_limit) {
+      atomicAdd(P.hbh.pop + r, ~0ull);  // undo: the ring is empty this iteration
+      err |= ERR_HISTORY;
+      return -1;
+    }
+    return __ldcg(P.hbh.ring + static_cast<size_t>(r) * P.hbh.nblocks + i % P.hbh.nblocks);
+  }
+  __device__ void hbh_push(int b) {
+    const int r = hbh_push_ring;
+    const unsigned long long i = atomicAdd(P.hbh.push + r, 1ull);
+    __stcg(P.hbh.ring + static_cast<size_t>(r) * P.hbh.nblocks + i % P.hbh.nblocks, b);
+  }
+  // A new history: its head block, with no particle counted yet.
+  __device__ void hbh_start() {
+    emitted = 0;
+    hblk = hbh_pop();
+    if (hblk < 0) return;
+    HbhBlock<R> *b = P.hbh.blocks + hblk;
+    __stcg(&b->count, 0);
+    __stcg(&b->next, -1);
+    __stcg(&b->live, 0);
+    __stcg(&b->slot, slot);
+  }
+  // Append (region, energy) to the history's chain; a full block gets a
+  // continuation block (the first lane to install one wins, the others
+  // return theirs).
+  __device__ void hbh_append(int ir, R x) {
+    int b = hblk;
+    for (int guard = 0; b >= 0 && guard < 1024; guard++) {
+      HbhBlock<R> *blk = P.hbh.blocks + b;
+      const int i = atomicAdd(&blk->count, 1);
+      if (i < HbhBlock<R>::kEntries) {
+        __stcg(&blk->ir[i], ir);
+        __stcg(&blk->x[i], x);
+        return;
+      }
+      int nb = *static_cast<volatile int *>(&blk->next);
+      if (nb < 0) {
+        const int cand = hbh_pop();
+        if (cand < 0) return;  // pool empty: this deposit is missing from the history sums (flagged)
+        HbhBlock<R> *c = P.hbh.blocks + cand;
+        __stcg(&c->count, 0);
+        __stcg(&c->next, -1);
+        __threadfence();
+        const int old = atomicCAS(&blk->next, -1, cand);
+        if (old == -1) {
+          nb = cand;
+        } else {
+          hbh_push(cand);
+          nb = old;
+        }
+      }
+      b = nb;
+    }
+    err |= ERR_HISTORY;
+  }
+  // End of a take (consumed = 1) or of an injection (consumed = 0): the
+  // history's particle count changes by emitted - consumed; at zero the
+  // history is complete and this lane merges it.
+  __device__ void hbh_finish(int consumed) {
+    if (hblk < 0) return;
+    const int delta = emitted - consumed;
+    emitted = 0;
+    if (delta == 0) return;
+    __threadfence();  // this lane's appends before the count
+    const int left = atomicAdd(&P.hbh.blocks[hblk].live, delta) + delta;
+    if (left == 0) {
+      __threadfence();  // every other lane's appends before the merge
+      hbh_merge(hblk);
+    }
+    hblk = -1;
+  }
+  // Sum the chain's entries per region in a local open-addressing table and
+  // score each region's total x as x (sum) and x^2 (sum2); return the
+  // blocks.  A history over 3/4 of the table's regions is merged in parts
+  // (its parts score as separate histories; counted in split).
+  __device__ void hbh_merge(int head) {
+    int kir[kHbhRegions];
+    double kx[kHbhRegions];
+    for (int k = 0; k < kHbhRegions; k++) kir[k] = -1;
+    int nd = 0;
+    int b = head;
+    for (int guard = 0; b >= 0 && guard < (1 << 20); guard++) {
+      HbhBlock<R> *blk = P.hbh.blocks + b;
+      const int n = min(__ldcg(&blk->count), HbhBlock<R>::kEntries);
+      for (int i = 0; i < n; i++) {
+        const int ir = __ldcg(&blk->ir[i]);
+        const double x = static_cast<double>(__ldcg(&blk->x[i]));
+        unsigned h = (static_cast<unsigned>(ir) * 2654435761u) >> 25;  // 7 bits: kHbhRegions = 128
+        for (;;) {
+          if (kir[h] == ir) {
+            kx[h] += x;
+            break;
+          }
+          if (kir[h] < 0) {
+            if (nd == kHbhRegions * 3 / 4) {
+              hbh_score_table(kir, kx);
+              nd = 0;
+              hbh_split++;
+            }
+            kir[h] = ir;
+            kx[h] = x;
+            nd++;
+            break;
+          }
+          h = (h + 1) & (kHbhRegions - 1);
+        }
+      }
+      const int nb = __ldcg(&blk->next);
+      hbh_push(b);
+      b = nb;
+    }
+    hbh_score_table(kir, kx);
+    hbh_merged++;
+  }
+  __device__ void hbh_score_table(int *kir, double *kx) {
+    for (int k = 0; k < kHbhRegions; k++) {
+      if (kir[k] < 0) continue;
+      atomicAdd(P.hbh.sum + kir[k], kx[k]);
+      atomicAdd(P.hbh.sum2 + kir[k], kx[k] * kx[k]);
+      kir[k] = -1;
+    }
   }
 
   // ---- geometry: region decode, howfar, hownear (omc_dosxyz.c:187-334) ----
