@@ -33,8 +33,12 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # -ffp-contract=off: the host table builders must round exactly like the
 # reference on every host architecture (no fused multiply-adds).
 CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function", f"-I{INCLUDE}"]
+# --use_fast_math changes single-precision arithmetic only (approximate division, square root and
+# transcendental intrinsics, denormals flushed): the FP32 transport path.  The FP64 path, and with it the
+# serial lane that reproduces the reference's serial build, is unchanged.  Measured on the 6 MV slab: FP32
+# 5.17e7 -> 7.21e7 histories/s, with the FP32-vs-FP64 dose error unchanged (bench.py fp32_dose_error).
 NVCCFLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", f"-I{INCLUDE}",
-                    "-Xptxas", "-warn-spills", "--expt-relaxed-constexpr"]
+                    "-Xptxas", "-warn-spills", "--expt-relaxed-constexpr", "--use_fast_math"]
 # Extra -D definitions for tuning builds (e.g. OMC_NVCC_DEFINES="OMC_MIN_BLOCKS_FP32=5").
 NVCCFLAGS += [f"-D{d}" for d in os.environ.get("OMC_NVCC_DEFINES", "").split() if d]
 
