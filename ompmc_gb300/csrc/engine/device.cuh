@@ -180,13 +180,14 @@ constexpr int kBatchTag = 4096;
 // history in flight owns a chain of blocks from a pool; its particles carry
 // the head block in their queue tag, each deposit appends (region, energy)
 // to the chain, and the head block counts the history's particles in flight.
-// The lane whose take brings that count to zero merges the chain by region
-// and adds the history's energy x in each region to sum[r] and x^2 to
-// sum2[r] -- the history-by-history estimators of Walters, Kawrakow and
-// Rogers (Med. Phys. 29 (2002) 2745) -- then returns the blocks.  Blocks
-// of 384 bytes: a 16-byte header and (region, energy) entries.
+// When a take brings that count to zero, the lane's warp merges the chain
+// by region (all 32 lanes on one history, in a shared-memory table) and
+// adds the history's energy x in each region to sum[r] and x^2 to sum2[r]
+// -- the history-by-history estimators of Walters, Kawrakow and Rogers
+// (Med. Phys. 29 (2002) 2745) -- then returns the blocks.  Blocks of 384
+// bytes: a 16-byte header and (region, energy) entries.
 constexpr int kHbhBlockBytes = 384;
-constexpr int kHbhRegions = 128;  // distinct regions a history merges at once (local table)
+constexpr int kHbhRegions = 128;  // distinct regions of one history the warp's merge table holds
 template <typename R>
 struct HbhBlock {
   static constexpr int kEntries = (kHbhBlockBytes - 16) / static_cast<int>(4 + sizeof(R));
@@ -198,17 +199,17 @@ struct HbhBlock {
   R x[kEntries];
 };
 
-// Free blocks: two rings of block ids, each with pop and push counters.
-// In wavefront iteration it, blocks are returned to ring it & 1 and taken
-// from the other ring, so no ring is pushed and popped at once and a pop
-// never reads an entry that a push is still writing.
+// Free blocks: a ring of block ids with a push and a pop counter.  A pop
+// in a wavefront iteration only takes entries pushed before the iteration
+// began (their writes are complete), so it never reads an entry that a
+// concurrent push is writing; the ring never holds more than nblocks ids,
+// so a push never overwrites an entry that is still to be popped.
 template <typename R>
 struct HbhPool {
   HbhBlock<R> *blocks;
   int nblocks;
-  int *ring;                  // [2][nblocks]
-  unsigned long long *pop;    // [2] ids taken from each ring
-  unsigned long long *push;   // [2] ids returned to each ring
+  int *ring;                  // [nblocks]
+  unsigned long long *ctr;    // {ids pushed, ids popped}
   double *sum, *sum2;         // [nreg] sums over histories of x and x^2
   unsigned long long *histories;  // histories merged
   unsigned long long *split;      // histories merged in parts (over the local region table)

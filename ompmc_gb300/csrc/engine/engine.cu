@@ -44,6 +44,10 @@ struct Occupancy {
   static constexpr int kMinBlocks = sizeof(R) == 4 ? OMC_MIN_BLOCKS_FP32 : OMC_MIN_BLOCKS_FP64;
 };
 constexpr int kDefaultDepth = 48;
+// History-by-history block pool: blocks per particle in flight, times 2.
+#ifndef OMC_HBH_POOL_X2
+#define OMC_HBH_POOL_X2 6
+#endif
 
 #define CUDA_TRY(expr)                                                                           \
   do {                                                                                           \
@@ -180,9 +184,9 @@ struct Wavefront {
   int trace_cap;              // iterations the trace holds
   int chunk_events;           // electron steps per take before re-queueing
   unsigned long long drain_below;  // drain mode below this many particles in flight
-  // history-by-history scoring: free blocks of the next iteration's pop
-  // ring (a lower bound, [2] by iteration parity) and the blocks an
-  // iteration keeps back for continuation blocks
+  // history-by-history scoring: pool counters {pushed, popped} as an
+  // iteration ended ([2][2] by iteration parity, written in the barrier)
+  // and the blocks an iteration keeps back for continuation blocks
   unsigned long long *hbh_free;
   unsigned long long hbh_reserve;
 };
@@ -209,7 +213,12 @@ constexpr long long kBarrierSpinCap = 1ll << 28;  // x ~64 ns: well past any pha
 // Grid-wide barrier for a cooperative launch (all blocks co-resident).  The
 // wait is bounded: on timeout the error flag is set and the block goes on,
 // so the kernel always ends.
-__device__ bool grid_barrier(unsigned *arrive, unsigned *gen, unsigned nblocks) {
+// snap_src/snap_dst (optional): the last block to arrive -- when every
+// other block has finished the iteration -- copies two counters to
+// snap_dst before it releases the others, so the next iteration reads
+// values that no thread changes any more.
+__device__ bool grid_barrier(unsigned *arrive, unsigned *gen, unsigned nblocks,
+                             const unsigned long long *snap_src = nullptr, unsigned long long *snap_dst = nullptr) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -218,6 +227,11 @@ __device__ bool grid_barrier(unsigned *arrive, unsigned *gen, unsigned nblocks) 
     unsigned g = *vgen;
     __threadfence();
     if (atomicAdd(arrive, 1u) == nblocks - 1) {
+      if (snap_src) {
+        __threadfence();
+        snap_dst[0] = *static_cast<const volatile unsigned long long *>(snap_src);
+        snap_dst[1] = *static_cast<const volatile unsigned long long *>(snap_src + 1);
+      }
       atomicExch(arrive, 0u);
       __threadfence();
       atomicAdd(gen, 1u);
@@ -248,6 +262,13 @@ __global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) wavefront_ke
   RngPlanes sp = rng_planes(s_raw);
   rng_to_smem(P.rng_u, P.nlanes, gtid, sp, t);
   Lane<R, true, MULTI, HBH> L(P, gtid, sp.lo + t, sp.hi + t, kBlock);
+  if constexpr (HBH) {
+    // Each warp's table for merging a completed history's deposits.
+    __shared__ int s_hir[kBlock / 32][kHbhRegions];
+    __shared__ double s_hx[kBlock / 32][kHbhRegions];
+    L.hbh_tir = s_hir[t >> 5];
+    L.hbh_tx = s_hx[t >> 5];
+  }
   L.rng.i = P.rng_ijc[gtid];
   L.rng.j = P.rng_ijc[P.nlanes + gtid];
   L.rng.c = P.rng_ijc[2 * P.nlanes + gtid];
@@ -285,14 +306,15 @@ __global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) wavefront_ke
     if (m < 0) m = 0;
     if (m > remaining) m = remaining;
     if constexpr (HBH) {
-      // Blocks are returned to ring it & 1 and taken from the other one,
-      // whose push count does not move during this iteration.  A new
-      // history needs a head block; some are kept for continuations.
-      L.hbh_push_ring = it & 1;
-      L.hbh_pop_ring = bout;
-      L.hbh_pop_limit = *static_cast<volatile unsigned long long *>(P.hbh.push + bout);
-      const long long nfree = static_cast<long long>(*static_cast<volatile unsigned long long *>(W.hbh_free + bin)) -
-                              static_cast<long long>(W.hbh_reserve);
+      // Pool counters as the last iteration ended (snapshot taken in the
+      // barrier): ring entries below the push count are written, and the
+      // free blocks are exact.  A new history needs a head block; some
+      // blocks are kept for continuations.
+      const unsigned long long *snap = W.hbh_free + 2 * bin;
+      const unsigned long long pushed = *static_cast<const volatile unsigned long long *>(snap);
+      const unsigned long long popped = *static_cast<const volatile unsigned long long *>(snap + 1);
+      L.hbh_pop_limit = pushed;
+      const long long nfree = static_cast<long long>(pushed - popped) - static_cast<long long>(W.hbh_reserve);
       if (m > nfree) m = nfree > 0 ? nfree : 0;
     }
     if (gtid == 0) {
@@ -388,18 +410,14 @@ __global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) wavefront_ke
           if constexpr (HBH) L.hbh_finish(1);
         }
       }
+      // Every lane of the warp is here (a chunk is one code path): the warp
+      // merges the histories its lanes just completed.
+      if constexpr (HBH) L.hbh_warp_merge();
     }
-    if constexpr (HBH) {
-      // Free blocks of the next iteration's pop ring (the ring this one
-      // fills): its pops are final, its pushes can only grow after this
-      // read, so the difference is a lower bound for every thread.
-      if (gtid == 0) {
-        const int nr = it & 1;
-        W.hbh_free[bout] = *static_cast<volatile unsigned long long *>(P.hbh.push + nr) -
-                           *static_cast<volatile unsigned long long *>(P.hbh.pop + nr);
-      }
-    }
-    if (!grid_barrier(W.bar_arrive, W.bar_gen, gridDim.x)) L.err |= ERR_BARRIER;
+    bool bar_ok;
+    if constexpr (HBH) bar_ok = grid_barrier(W.bar_arrive, W.bar_gen, gridDim.x, P.hbh.ctr, W.hbh_free + 2 * bout);
+    else bar_ok = grid_barrier(W.bar_arrive, W.bar_gen, gridDim.x);
+    if (!bar_ok) L.err |= ERR_BARRIER;
   }
   if (it >= W.max_iters) L.err |= ERR_LOOP;
   rng_from_smem(P.rng_u, P.nlanes, gtid, sp, t);
@@ -1071,22 +1089,21 @@ int wavefront_blocks(omc_engine *e) {
 
 // Counters of the history-by-history pool (one device buffer).
 struct HbhCounters {
-  unsigned long long pop[2], push[2];
-  unsigned long long free[2];  // Wavefront::hbh_free
+  unsigned long long ctr[2];   // {pushed, popped}: HbhPool::ctr
+  unsigned long long snap[4];  // Wavefront::hbh_free
   unsigned long long histories, split;
 };
 
-// A full pool: every block id in ring 1, which iteration 0 pops.
+// A full pool: every block id in the ring.
 __global__ void hbh_init_kernel(int *ring, int nblocks, HbhCounters *c) {
   for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < nblocks;
        i += static_cast<long long>(gridDim.x) * blockDim.x)
-    ring[nblocks + i] = static_cast<int>(i);
+    ring[i] = static_cast<int>(i);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    c->pop[0] = c->pop[1] = 0;
-    c->push[0] = 0;
-    c->push[1] = static_cast<unsigned long long>(nblocks);
-    c->free[0] = static_cast<unsigned long long>(nblocks);
-    c->free[1] = 0;
+    c->ctr[0] = static_cast<unsigned long long>(nblocks);
+    c->ctr[1] = 0;
+    c->snap[0] = static_cast<unsigned long long>(nblocks);  // iteration 0 reads slot 0
+    c->snap[1] = 0;
   }
 }
 
@@ -1178,23 +1195,23 @@ omc_status run_wavefront(omc_engine *e, PrecisionState<R> &S, const omc_run_conf
   HbhCounters *hc_dev = nullptr;
   int hbh_nblocks = 0;
   if (hbh) {
-    const unsigned long long nb = target + target / 2 + 8ull * nlanes;
+    const unsigned long long nb = target * OMC_HBH_POOL_X2 / 2 + 8ull * nlanes;
     if (nb > 0x7fffffffull) return fail(OMC_ERR_ARG, "history tracking: %llu blocks exceed the pool index", nb);
     hbh_nblocks = static_cast<int>(nb);
     if (e->hbh_blocks.ensure(nb * sizeof(HbhBlock<R>)) != OMC_OK) return OMC_ERR_NOMEM;
-    if (e->hbh_ring.ensure(2 * nb * sizeof(int)) != OMC_OK) return OMC_ERR_NOMEM;
+    if (e->hbh_ring.ensure(nb * sizeof(int)) != OMC_OK) return OMC_ERR_NOMEM;
     if (e->hbh_ctr.ensure(sizeof(HbhCounters)) != OMC_OK) return OMC_ERR_NOMEM;
     hc_dev = static_cast<HbhCounters *>(e->hbh_ctr.p);
+    CUDA_TRY(cudaMemsetAsync(hc_dev, 0, sizeof(HbhCounters), e->stream));
     P.hbh.blocks = static_cast<HbhBlock<R> *>(e->hbh_blocks.p);
     P.hbh.nblocks = hbh_nblocks;
     P.hbh.ring = static_cast<int *>(e->hbh_ring.p);
-    P.hbh.pop = hc_dev->pop;
-    P.hbh.push = hc_dev->push;
+    P.hbh.ctr = hc_dev->ctr;
     P.hbh.sum = static_cast<double *>(e->hbh_sum.p);
     P.hbh.sum2 = static_cast<double *>(e->hbh_sum2.p);
     P.hbh.histories = &hc_dev->histories;
     P.hbh.split = &hc_dev->split;
-    W.hbh_free = hc_dev->free;
+    W.hbh_free = hc_dev->snap;
     W.hbh_reserve = 4ull * nlanes;
   }
   const int nlaunch = job ? 1 : cfg->nbatch;

@@ -54,6 +54,11 @@ __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, 
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+// Correctly rounded quotient and square root, also in a fast-math build.
+__device__ __forceinline__ float div_rn(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double div_rn(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ float sqrt_rn(float a) { return __fsqrt_rn(a); }
+__device__ __forceinline__ double sqrt_rn(double a) { return __dsqrt_rn(a); }
 
 // Output queues of the current wavefront phase.
 template <typename R>
@@ -105,11 +110,15 @@ struct Lane {
   unsigned long long n_dep;   // ausgab calls (energy deposits)
   // history-by-history scoring (HBH): head block of the current particle's
   // history (-1: not tracked), particles emitted by the current take, the
-  // rings of this iteration and the ids the pop ring holds
+  // ring entries written before this iteration began, a history this lane
+  // completed and its warp is to merge (-1: none), and the warp's merge
+  // table in shared memory
   int hblk = -1;
   int emitted = 0;
-  int hbh_pop_ring = 1, hbh_push_ring = 0;
   unsigned long long hbh_pop_limit = 0;
+  int hbh_done = -1;
+  int *hbh_tir = nullptr;
+  double *hbh_tx = nullptr;
   unsigned long long hbh_merged = 0, hbh_split = 0;
 
   __device__ Lane(const Params<R> &prm, int ln, unsigned short *slo, unsigned char *shi, int sstride)
@@ -299,19 +308,17 @@ struct Lane {
 
   // ---- history-by-history scoring (HBH) --------------------------------------
   __device__ int hbh_pop() {
-    const int r = hbh_pop_ring;
-    const unsigned long long i = atomicAdd(P.hbh.pop + r, 1ull);
+    const unsigned long long i = atomicAdd(P.hbh.ctr + 1, 1ull);
     if (i >= hbh_pop_limit) {
-      atomicAdd(P.hbh.pop + r, ~0ull);  // undo: the ring is empty this iteration
+      atomicAdd(P.hbh.ctr + 1, ~0ull);  // undo: no entry written before this iteration is left
       err |= ERR_HISTORY;
       return -1;
     }
-    return __ldcg(P.hbh.ring + static_cast<size_t>(r) * P.hbh.nblocks + i % P.hbh.nblocks);
+    return __ldcg(P.hbh.ring + i % P.hbh.nblocks);
   }
   __device__ void hbh_push(int b) {
-    const int r = hbh_push_ring;
-    const unsigned long long i = atomicAdd(P.hbh.push + r, 1ull);
-    __stcg(P.hbh.ring + static_cast<size_t>(r) * P.hbh.nblocks + i % P.hbh.nblocks, b);
+    const unsigned long long i = atomicAdd(P.hbh.ctr, 1ull);
+    __stcg(P.hbh.ring + i % P.hbh.nblocks, b);
   }
   // A new history: its head block, with no particle counted yet.
   __device__ void hbh_start() {
@@ -359,7 +366,7 @@ struct Lane {
   }
   // End of a take (consumed = 1) or of an injection (consumed = 0): the
   // history's particle count changes by emitted - consumed; at zero the
-  // history is complete and this lane merges it.
+  // history is complete, and this lane hands it to its warp's merge.
   __device__ void hbh_finish(int consumed) {
     if (hblk < 0) return;
     const int delta = emitted - consumed;
@@ -369,59 +376,72 @@ struct Lane {
     const int left = atomicAdd(&P.hbh.blocks[hblk].live, delta) + delta;
     if (left == 0) {
       __threadfence();  // every other lane's appends before the merge
-      hbh_merge(hblk);
+      hbh_done = hblk;
     }
     hblk = -1;
   }
-  // Sum the chain's entries per region in a local open-addressing table and
-  // score each region's total x as x (sum) and x^2 (sum2); return the
-  // blocks.  A history over 3/4 of the table's regions is merged in parts
-  // (its parts score as separate histories; counted in split).
-  __device__ void hbh_merge(int head) {
-    int kir[kHbhRegions];
-    double kx[kHbhRegions];
-    for (int k = 0; k < kHbhRegions; k++) kir[k] = -1;
-    int nd = 0;
-    int b = head;
-    for (int guard = 0; b >= 0 && guard < (1 << 20); guard++) {
-      HbhBlock<R> *blk = P.hbh.blocks + b;
-      const int n = min(__ldcg(&blk->count), HbhBlock<R>::kEntries);
-      for (int i = 0; i < n; i++) {
-        const int ir = __ldcg(&blk->ir[i]);
-        const double x = static_cast<double>(__ldcg(&blk->x[i]));
-        unsigned h = (static_cast<unsigned>(ir) * 2654435761u) >> 25;  // 7 bits: kHbhRegions = 128
-        for (;;) {
-          if (kir[h] == ir) {
-            kx[h] += x;
-            break;
-          }
-          if (kir[h] < 0) {
-            if (nd == kHbhRegions * 3 / 4) {
-              hbh_score_table(kir, kx);
-              nd = 0;
-              hbh_split++;
-            }
-            kir[h] = ir;
-            kx[h] = x;
-            nd++;
-            break;
-          }
-          h = (h + 1) & (kHbhRegions - 1);
-        }
+  // The warp merges the histories its lanes completed, one after another
+  // and all 32 lanes on each: the lanes load a block's entries together and
+  // sum them per region in the warp's shared-memory table, then score each
+  // region's total x as x (sum) and x^2 (sum2) and return the blocks.  A
+  // history over the table's regions is scored in parts (counted in split).
+  // Called by all 32 lanes of the warp at the same point.
+  __device__ void hbh_warp_merge() {
+    const unsigned full = 0xffffffffu;
+    const int lane_id = threadIdx.x & 31;
+    unsigned pending = __ballot_sync(full, hbh_done >= 0);
+    while (pending) {
+      const int src = __ffs(pending) - 1;
+      pending &= pending - 1;
+      const int head = __shfl_sync(full, hbh_done, src);
+      for (int k = lane_id; k < kHbhRegions; k += 32) {
+        hbh_tir[k] = -1;
+        hbh_tx[k] = 0.0;
       }
-      const int nb = __ldcg(&blk->next);
-      hbh_push(b);
-      b = nb;
-    }
-    hbh_score_table(kir, kx);
-    hbh_merged++;
-  }
-  __device__ void hbh_score_table(int *kir, double *kx) {
-    for (int k = 0; k < kHbhRegions; k++) {
-      if (kir[k] < 0) continue;
-      atomicAdd(P.hbh.sum + kir[k], kx[k]);
-      atomicAdd(P.hbh.sum2 + kir[k], kx[k] * kx[k]);
-      kir[k] = -1;
+      __syncwarp();
+      bool split = false;
+      int b = head;
+      for (int guard = 0; b >= 0 && guard < (1 << 20); guard++) {
+        const HbhBlock<R> *blk = P.hbh.blocks + b;
+        const int n = min(__ldcg(&blk->count), HbhBlock<R>::kEntries);
+        const int nb = __ldcg(&blk->next);
+        for (int i = lane_id; i < n; i += 32) {
+          const int ir = __ldcg(&blk->ir[i]);
+          const double x = static_cast<double>(__ldcg(&blk->x[i]));
+          unsigned h = (static_cast<unsigned>(ir) * 2654435761u) >> 25;  // 7 bits: kHbhRegions = 128
+          int probe = 0;
+          for (; probe < kHbhRegions; probe++) {
+            const int old = atomicCAS(hbh_tir + h, -1, ir);
+            if (old == -1 || old == ir) {
+              atomicAdd(hbh_tx + h, x);
+              break;
+            }
+            h = (h + 1) & (kHbhRegions - 1);
+          }
+          if (probe == kHbhRegions) {  // table full: this deposit scores as a part of its own
+            atomicAdd(P.hbh.sum + ir, x);
+            atomicAdd(P.hbh.sum2 + ir, x * x);
+            split = true;
+          }
+        }
+        if (lane_id == 0) hbh_push(b);
+        b = nb;
+      }
+      __syncwarp();
+      for (int k = lane_id; k < kHbhRegions; k += 32) {
+        const int ir = hbh_tir[k];
+        if (ir < 0) continue;
+        const double x = hbh_tx[k];
+        atomicAdd(P.hbh.sum + ir, x);
+        atomicAdd(P.hbh.sum2 + ir, x * x);
+      }
+      __syncwarp();
+      split = __any_sync(full, split);
+      if (lane_id == src) {
+        hbh_done = -1;
+        hbh_merged++;
+        if (split) hbh_split++;
+      }
     }
   }
 
@@ -665,7 +685,8 @@ struct Lane {
   // against ybounds[0] (:1225); that is kept.  A point that lands a
   // rounding error below zbounds[0] is moved by that clamp, so the
   // arithmetic here is rounded operation by operation like the
-  // reference's (no fused multiply-adds).
+  // reference's: no fused multiply-adds, and correctly rounded division
+  // and square root.
   __device__ void init_beamlet_history(int ib) {
     const Source<R> &s = src();
     const Geometry<R> &g = geo();
@@ -679,34 +700,34 @@ struct Lane {
     R ziso = add_rn(add_rn(mul_rn(rnno1, __ldg(b + 5)), mul_rn(rnno2, __ldg(b + 8))), __ldg(b + 2));
     const R *src = s.beam_src + 3 * __ldg(s.ibeam + ib);
     R dx = xiso - __ldg(src + 0), dy = yiso - __ldg(src + 1), dz = ziso - __ldg(src + 2);
-    R vnorm = sqrt(add_rn(add_rn(mul_rn(dx, dx), mul_rn(dy, dy)), mul_rn(dz, dz)));
-    R u = -dx / vnorm, v = -dy / vnorm, w = -dz / vnorm;
+    R vnorm = sqrt_rn(add_rn(add_rn(mul_rn(dx, dx), mul_rn(dy, dy)), mul_rn(dz, dz)));
+    R u = div_rn(-dx, vnorm), v = div_rn(-dy, vnorm), w = div_rn(-dz, vnorm);
     R ustep = RC(1.0E5), dist;
     const R x0 = __ldg(g.xb), x1 = __ldg(g.xb + g.nx);
     const R y0 = __ldg(g.yb), y1 = __ldg(g.yb + g.ny);
     const R z0 = __ldg(g.zb), z1 = __ldg(g.zb + g.nz);
     if (u > RC(0)) {
-      dist = (x1 - xiso) / u;
+      dist = div_rn(x1 - xiso, u);
       if (dist < ustep) ustep = dist;
     }
     if (u < RC(0)) {
-      dist = -(xiso - x0) / u;
+      dist = div_rn(-(xiso - x0), u);
       if (dist < ustep) ustep = dist;
     }
     if (v > RC(0)) {
-      dist = (y1 - yiso) / v;
+      dist = div_rn(y1 - yiso, v);
       if (dist < ustep) ustep = dist;
     }
     if (v < RC(0)) {
-      dist = -(yiso - y0) / v;
+      dist = div_rn(-(yiso - y0), v);
       if (dist < ustep) ustep = dist;
     }
     if (w > RC(0)) {
-      dist = (z1 - ziso) / w;
+      dist = div_rn(z1 - ziso, w);
       if (dist < ustep) ustep = dist;
     }
     if (w < RC(0)) {
-      dist = -(ziso - z0) / w;
+      dist = div_rn(-(ziso - z0), w);
       if (dist < ustep) ustep = dist;
     }
     R x = add_rn(xiso, mul_rn(ustep, u)), y = add_rn(yiso, mul_rn(ustep, v)), z = add_rn(ziso, mul_rn(ustep, w));
