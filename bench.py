@@ -422,6 +422,25 @@ def run_ours(args, rank, world, local_rank, dist_on):
                            "by_max_s": T16 * (float(s16.max()) / 0.01) ** 2,
                            "by_mean_s": T16 * (float(s16.mean()) / 0.01) ** 2},
               "note": "T x (s/0.01)^2: s falls as 1/sqrt(histories); batch sigma (10 batches)"}
+        # the same workload with history-by-history scoring: s by history
+        # beside s by batch, over the same voxels
+        Hh = args.hbh_histories
+        ah, ah2, sth = eng.run(nperbatch=Hh // 10, nbatch=10, precision=api.FP32, history_stats=1,
+                               seeds=D.rank_seeds(3307, 51, rank, LANES_PER_RANK_STRIDE))
+        hs, hs2, h_merged, h_split = eng.history_sums()
+        Th = sth.kernel_ms / 1000.0
+        mh = hs[1:] / Hh
+        rel_h = np.sqrt(np.maximum(hs2[1:] / Hh - mh * mh, 0.0) / (Hh - 1))[sel50] / mh[sel50]
+        rel_b = rel_sigmas(ah, ah2, 10, sel50)
+        hbh = {"histories": Hh, "T_s": Th, "histories_per_s": Hh / Th, "merged": h_merged, "split": h_split,
+               "error_flags": int(sth.error_flags),
+               "s_max": float(rel_h.max()), "s_mean": float(rel_h.mean()),
+               "s_max_batch": float(rel_b.max()), "s_mean_batch": float(rel_b.mean()),
+               "time_to_1pct_by_max_s": Th * (float(rel_h.max()) / 0.01) ** 2,
+               "time_to_1pct_by_mean_s": Th * (float(rel_h.mean()) / 0.01) ** 2,
+               "note": "history-by-history sums of x and x^2 per voxel (omc_engine_history_sums) on a run of its "
+                       "own; s = relative sigma of the mean over the voxels above 50% of Dmax; the time to 1% "
+                       "is that run's time scaled by (s/0.01)^2"}
         # end to end through the C ABI: phantom upload, the K-batch job,
         # batch sums back in host memory
         ph = prob.phantom
@@ -472,6 +491,7 @@ def run_ours(args, rank, world, local_rank, dist_on):
                 "efficiency": {"value": efficiency, "unit": "1/(s^2*T)", "s_max_rel_above_50pct": s,
                                "T_s": T},
                 "time_to_1pct": t1,
+                "history_by_history": hbh,
                 "serving": serving,
                 "job_ms": dev_ms,
                 "per_history": {"events": evs / (K * H), "voxel_steps": geo / (K * H),
@@ -596,11 +616,13 @@ CT_WORKLOAD = ("CT-like blob phantom 256x256x128 @ 2 mm (seed 2024), synthetic 6
 
 def run_ct_leg(args, local_rank):
     """FP32-transport dose error against an FP64 run of the same engine, per
-    field, on the CT-like phantom: both precisions with the same histories
-    in 10 batches; per-voxel z over voxels above 20% of Dmax (t-corrected),
-    mean relative difference over voxels above 50% of Dmax, total energy."""
+    field, on the CT-like phantom: both precisions with the same histories in
+    10 batches, on disjoint streams; the statement of fp32_dose_error (per
+    voxel z over voxels above 20% of Dmax; mean dose over voxels above 50%
+    of Dmax and total energy, each with a sigma from the per-batch sums of
+    both runs, so voxel correlations are included).  The voxels are chosen on
+    a separate FP32 run."""
     import torch
-    from scipy import stats as S
 
     from ompmc_gb300 import api, data
     from ompmc_gb300 import workloads as W
@@ -626,33 +648,23 @@ def run_ct_leg(args, local_rank):
                 prob = api.Problem(api.Input(text=job.text()), phantom=phantom)
                 eng = api.Engine(local_rank).load(prob)
                 f = dose_factor(prob)
-                eng.run(nperbatch=100000, nbatch=1, precision=api.FP32)  # warm-up
+                sel_acc, _, _ = eng.run(nperbatch=H // 2, nbatch=1, precision=api.FP32, seeds=(3001, 5))
+                dsel = sel_acc[1:] * f
+                sel20 = dsel > 0.2 * dsel.max()
+                sel50 = dsel > 0.5 * dsel.max()
+                w_roi = np.concatenate([[0.0], np.where(sel50, f, 0.0)])
+                w_in = np.concatenate([[0.0], np.ones(prob.nreg - 1)])
                 a32, b32, s32 = eng.run(precision=api.FP32, seeds=(97, 33))
+                roi32, tot32 = eng.batch_sums(w_roi), eng.batch_sums(w_in)
                 a64, b64, s64 = eng.run(precision=api.FP64, seeds=(12, 34))
+                roi64, tot64 = eng.batch_sums(w_roi), eng.batch_sums(w_in)
                 eng.close()
-                m32, m64 = a32[1:] / nb, a64[1:] / nb
-                v32 = np.maximum(b32[1:] / nb - m32 ** 2, 0) / (nb - 1)
-                v64 = np.maximum(b64[1:] / nb - m64 ** 2, 0) / (nb - 1)
-                # Voxels are selected on the dose of the mean of both runs:
-                # selecting on one run alone picks voxels where that run
-                # fluctuated upwards.  The z-scores and ratios below are per
-                # voxel, so energy or dose gives the same values.
-                dm = 0.5 * (m32 + m64) * f
-                sel = dm > 0.2 * dm.max()
-                tz = (m32[sel] - m64[sel]) / np.sqrt(v32[sel] + v64[sel])
-                z = S.norm.ppf(np.clip(S.t.cdf(tz, 2 * (nb - 1)), 1e-300, 1 - 1e-16))
-                hi = dm > 0.5 * dm.max()
-                d32, d64 = m32 * f, m64 * f
-                fields.append({"field": f"{gname} {2 * half:g}x{2 * half:g} cm2", "histories": H,
-                               "fp32_histories_per_s": H / (s32.kernel_ms / 1e3),
-                               "fp64_histories_per_s": H / (s64.kernel_ms / 1e3),
-                               "voxels_above_20pct": int(sel.sum()),
-                               "frac_within_2sigma": float(np.mean(np.abs(z) <= 2)),
-                               "mean_z2": float(np.mean(z * z)),
-                               "dose_rel_diff_above_50pct": float(d32[hi].sum() / d64[hi].sum() - 1),
-                               "sigma_independent_voxels": float(np.sqrt(((v32[hi] + v64[hi]) * f[hi] ** 2).sum())
-                                                                 / d64[hi].sum()),
-                               "total_energy_rel_diff": float(a32[1:].sum() / a64[1:].sum() - 1)})
+                err = fp32_dose_error(a32, b32, H // nb, nb, roi32, tot32, a64, b64, H // nb, nb, roi64, tot64, f,
+                                      sel20)
+                err.update({"field": f"{gname} {2 * half:g}x{2 * half:g} cm2", "histories": H,
+                            "fp32_histories_per_s": H / (s32.kernel_ms / 1e3),
+                            "fp64_histories_per_s": H / (s64.kernel_ms / 1e3)})
+                fields.append(err)
     return {"metric": "FP32-transport dose error vs FP64, per field", "n_gpus": 1, "data": "synthetic",
             "config": {"workload": CT_WORKLOAD, "batches": nb}, "fields": fields}
 
@@ -802,6 +814,8 @@ def main():
     ap.add_argument("--no-serving", action="store_true", help="leave the short serving run out of the default line")
     ap.add_argument("--fp64-histories", type=int, default=FP64_HISTORIES)
     ap.add_argument("--nsplit16-histories", type=int, default=NSPLIT16_HISTORIES)
+    ap.add_argument("--hbh-histories", type=int, default=20_000_000,
+                    help="histories of the history-by-history run (10 batches)")
     ap.add_argument("--inflight", type=int, default=0,
                     help="particles in flight (0 = the engine's default); smaller values only to keep the device "
                          "memory of profiler captures small")
