@@ -30,14 +30,15 @@ constexpr int kBlock = 128;  // lanes per block
 // Shared memory of a block: the RANMAR states of its lanes, 3 bytes a word.
 constexpr size_t kRngSmem = static_cast<size_t>(RNG_WORDS) * kBlock * 3;
 // Blocks per SM the register budget is sized for (measured on the 6 MV
-// slab): FP32 5 blocks, up to 102 registers, beat 6 blocks, 80 registers
-// and spilling, by 18% although shared memory would allow 6; FP64 2 blocks
-// beat 3 by 3%.
+// slab, fast-math build with one-pass electron events): FP32 5 blocks (96
+// registers) 7.96e7 hist/s, against 7.48e7 with 4 and 6.73e7 with 6 (80
+// registers and spilling); FP64 3 blocks (168 registers) 4.17e6, against
+// 4.00e6 with 2.
 #ifndef OMC_MIN_BLOCKS_FP32
 #define OMC_MIN_BLOCKS_FP32 5
 #endif
 #ifndef OMC_MIN_BLOCKS_FP64
-#define OMC_MIN_BLOCKS_FP64 2
+#define OMC_MIN_BLOCKS_FP64 3
 #endif
 template <typename R>
 struct Occupancy {
