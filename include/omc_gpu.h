@@ -341,8 +341,9 @@ omc_status omc_engine_run_resident(omc_engine *e, const omc_run_config *cfg,
  * the merge table holds (they count as several histories; zero in
  * practice).  The reference has only the batch method (accumEndep,
  * omc_dosxyz.c:696-755), which every run still returns.  History tracking
- * needs a pool of about 1.5 * inflight blocks of 384 bytes on the device
- * during the run; OMC_ERR_STATE if the last run did not track histories. */
+ * needs a pool of 3 blocks of 384 bytes per particle in flight on the
+ * device during the run (14 GB at the FP32 default).  OMC_ERR_STATE if
+ * the last run did not track histories. */
 omc_status omc_engine_history_sums(omc_engine *e, double *sum, double *sum2,
                                    long long *histories, long long *split);
 

@@ -208,7 +208,8 @@ template <typename R>
 struct HbhPool {
   HbhBlock<R> *blocks;
   int nblocks;
-  int *ring;                  // [nblocks]
+  int *ring;                  // [ring_mask + 1], a power of two >= nblocks
+  unsigned ring_mask;
   unsigned long long *ctr;    // {ids pushed, ids popped}
   double *sum, *sum2;         // [nreg] sums over histories of x and x^2
   unsigned long long *histories;  // histories merged

@@ -1097,6 +1097,8 @@ struct HbhCounters {
 
 // A full pool: every block id in the ring.
 __global__ void hbh_init_kernel(int *ring, int nblocks, HbhCounters *c) {
+  // ring positions are taken modulo a power of two >= nblocks; the first
+  // nblocks hold every block id
   for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < nblocks;
        i += static_cast<long long>(gridDim.x) * blockDim.x)
     ring[i] = static_cast<int>(i);
@@ -1200,12 +1202,15 @@ omc_status run_wavefront(omc_engine *e, PrecisionState<R> &S, const omc_run_conf
     if (nb > 0x7fffffffull) return fail(OMC_ERR_ARG, "history tracking: %llu blocks exceed the pool index", nb);
     hbh_nblocks = static_cast<int>(nb);
     if (e->hbh_blocks.ensure(nb * sizeof(HbhBlock<R>)) != OMC_OK) return OMC_ERR_NOMEM;
-    if (e->hbh_ring.ensure(nb * sizeof(int)) != OMC_OK) return OMC_ERR_NOMEM;
+    unsigned long long ring = 1;
+    while (ring < nb) ring <<= 1;
+    if (e->hbh_ring.ensure(ring * sizeof(int)) != OMC_OK) return OMC_ERR_NOMEM;
     if (e->hbh_ctr.ensure(sizeof(HbhCounters)) != OMC_OK) return OMC_ERR_NOMEM;
     hc_dev = static_cast<HbhCounters *>(e->hbh_ctr.p);
     CUDA_TRY(cudaMemsetAsync(hc_dev, 0, sizeof(HbhCounters), e->stream));
     P.hbh.blocks = static_cast<HbhBlock<R> *>(e->hbh_blocks.p);
     P.hbh.nblocks = hbh_nblocks;
+    P.hbh.ring_mask = static_cast<unsigned>(ring - 1);
     P.hbh.ring = static_cast<int *>(e->hbh_ring.p);
     P.hbh.ctr = hc_dev->ctr;
     P.hbh.sum = static_cast<double *>(e->hbh_sum.p);

@@ -314,22 +314,40 @@ struct Lane {
       err |= ERR_HISTORY;
       return -1;
     }
-    return __ldcg(P.hbh.ring + i % P.hbh.nblocks);
+    return __ldcg(P.hbh.ring + (i & P.hbh.ring_mask));
   }
   __device__ void hbh_push(int b) {
     const unsigned long long i = atomicAdd(P.hbh.ctr, 1ull);
-    __stcg(P.hbh.ring + i % P.hbh.nblocks, b);
+    __stcg(P.hbh.ring + (i & P.hbh.ring_mask), b);
   }
-  // A new history: its head block, with no particle counted yet.
+  // A new history: its head block, with no particle counted yet.  The
+  // lanes that start histories together take their blocks with one atomic.
   __device__ void hbh_start() {
     emitted = 0;
-    hblk = hbh_pop();
-    if (hblk < 0) return;
-    HbhBlock<R> *b = P.hbh.blocks + hblk;
-    __stcg(&b->count, 0);
-    __stcg(&b->next, -1);
-    __stcg(&b->live, 0);
-    __stcg(&b->slot, slot);
+    const unsigned am = __activemask();
+    const int leader = __ffs(am) - 1;
+    const unsigned cnt = __popc(am);
+    unsigned long long b = 0;
+    if ((threadIdx.x & 31) == leader) {
+      b = atomicAdd(P.hbh.ctr + 1, static_cast<unsigned long long>(cnt));
+      if (b + cnt > hbh_pop_limit) {  // undo the ids that are not there this iteration
+        const unsigned long long over = b + cnt - (b > hbh_pop_limit ? b : hbh_pop_limit);
+        atomicAdd(P.hbh.ctr + 1, 0ull - over);
+      }
+    }
+    b = __shfl_sync(am, b, leader);
+    const unsigned long long i = b + __popc(am & lanemask_lt());
+    if (i >= hbh_pop_limit) {
+      err |= ERR_HISTORY;
+      hblk = -1;
+      return;
+    }
+    hblk = __ldcg(P.hbh.ring + (i & P.hbh.ring_mask));
+    HbhBlock<R> *h = P.hbh.blocks + hblk;
+    __stcg(&h->count, 0);
+    __stcg(&h->next, -1);
+    __stcg(&h->live, 0);
+    __stcg(&h->slot, slot);
   }
   // Append (region, energy) to the history's chain; a full block gets a
   // continuation block (the first lane to install one wins, the others
@@ -401,6 +419,7 @@ struct Lane {
       __syncwarp();
       bool split = false;
       int b = head;
+      int mine = -1;  // block `guard` of the chain when guard == this lane
       for (int guard = 0; b >= 0 && guard < (1 << 20); guard++) {
         const HbhBlock<R> *blk = P.hbh.blocks + b;
         const int n = min(__ldcg(&blk->count), HbhBlock<R>::kEntries);
@@ -424,8 +443,20 @@ struct Lane {
             split = true;
           }
         }
-        if (lane_id == 0) hbh_push(b);
+        if (guard < 32) {
+          if (lane_id == guard) mine = b;
+        } else if (lane_id == 0) {
+          hbh_push(b);  // chains over 32 blocks: the rest one by one
+        }
         b = nb;
+      }
+      // Return the chain's first 32 blocks with one atomic.
+      const unsigned have = __ballot_sync(full, mine >= 0);
+      if (have) {
+        unsigned long long base = 0;
+        if (lane_id == 0) base = atomicAdd(P.hbh.ctr, static_cast<unsigned long long>(__popc(have)));
+        base = __shfl_sync(full, base, 0);
+        if (mine >= 0) __stcg(P.hbh.ring + ((base + __popc(have & lanemask_lt())) & P.hbh.ring_mask), mine);
       }
       __syncwarp();
       for (int k = lane_id; k < kHbhRegions; k += 32) {
