@@ -170,9 +170,12 @@ struct Wavefront {
   R *pi_f[2];             // photons waiting for their interaction
   int *pi_k[2];
   int *pi_s[2];
+  R *eb_f[2];             // electrons within a skin depth of a boundary
+  int *eb_k[2];
+  int *eb_s[2];
   unsigned cap;           // slots per queue
   unsigned *ctr;          // [0..2] photon, [3..5] electron, [6..8] electron-interaction,
-                          // [9..11] photon-interaction counters
+                          // [9..11] photon-interaction, [12..14] boundary-electron counters
   unsigned long long *work;      // [3] chunk counters of the phase
   unsigned long long *injected;  // [2] histories injected before the iteration
   unsigned *bar_arrive;
@@ -289,16 +292,17 @@ __global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) wavefront_ke
     const unsigned n_el = vload(W.ctr + 3 + cin);
     const unsigned n_ei = vload(W.ctr + 6 + cin);
     const unsigned n_pi = vload(W.ctr + 9 + cin);
+    const unsigned n_eb = vload(W.ctr + 12 + cin);
     const unsigned long long injected = *static_cast<volatile unsigned long long *>(W.injected + bin);
     const long long remaining = P.nhist - static_cast<long long>(injected);
-    const unsigned long long inflight = static_cast<unsigned long long>(n_ph) + n_el + n_ei + n_pi;
+    const unsigned long long inflight = static_cast<unsigned long long>(n_ph) + n_el + n_ei + n_pi + n_eb;
     if (W.trace && gtid == 0 && it < W.trace_cap) {
       unsigned long long ns;
       asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(ns));
       unsigned long long *r = W.trace + 4 * static_cast<size_t>(it);
       r[0] = ns;
       r[1] = n_ph;
-      r[2] = n_el;
+      r[2] = n_el + n_eb;
       r[3] = injected;
     }
     if (remaining <= 0 && inflight == 0) break;
@@ -323,6 +327,7 @@ __global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) wavefront_ke
       W.ctr[3 + cfree] = 0;
       W.ctr[6 + cfree] = 0;
       W.ctr[9 + cfree] = 0;
+      W.ctr[12 + cfree] = 0;
       W.work[cfree] = 0;
       W.injected[bout] = injected + static_cast<unsigned long long>(m);
     }
@@ -332,18 +337,19 @@ __global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) wavefront_ke
     L.out = EmitTargets<R>{W.ph_f[bout], W.ph_k[bout], W.ctr + cout,     W.el_f[bout], W.el_k[bout],
                            W.ctr + 3 + cout, W.ph_s[bout], W.el_s[bout],     W.ei_f[bout], W.ei_k[bout],
                            W.ctr + 6 + cout, W.ei_s[bout], W.pi_f[bout],     W.pi_k[bout], W.ctr + 9 + cout,
-                           W.pi_s[bout]};
+                           W.pi_s[bout], W.eb_f[bout], W.eb_k[bout], W.ctr + 12 + cout, W.eb_s[bout]};
     // Chunk ranges of the phase in claim order [new histories | photon
-    // flights | photon interactions | electron steps | electron
-    // interactions], each padded to a multiple of 32 so that a warp's chunk
-    // is one code path.  (Claiming the electron steps first, largest work
-    // first, measured 3% slower.)
+    // flights | photon interactions | electron steps | electron steps near
+    // a boundary | electron interactions], each padded to a multiple of 32
+    // so that a warp's chunk is one code path.  (Claiming the electron
+    // steps first, largest work first, measured 3% slower.)
     const unsigned long long el_pad = (static_cast<unsigned long long>(n_el) + 31) & ~31ull;
     const unsigned long long ph_pad = (static_cast<unsigned long long>(n_ph) + 31) & ~31ull;
     const unsigned long long pi_pad = (static_cast<unsigned long long>(n_pi) + 31) & ~31ull;
     const unsigned long long ei_pad = (static_cast<unsigned long long>(n_ei) + 31) & ~31ull;
+    const unsigned long long eb_pad = (static_cast<unsigned long long>(n_eb) + 31) & ~31ull;
     const unsigned long long r_in = 0, r_ph = r_in + ((static_cast<unsigned long long>(m) + 31) & ~31ull),
-                             r_pi = r_ph + ph_pad, r_el = r_pi + pi_pad, r_ei = r_el + el_pad,
+                             r_pi = r_ph + ph_pad, r_el = r_pi + pi_pad, r_eb = r_el + el_pad, r_ei = r_eb + eb_pad,
                              total = r_ei + ei_pad;
     for (;;) {
       unsigned long long base = 0;
@@ -376,16 +382,19 @@ __global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) wavefront_ke
           L.deferred_photon_interaction(survivor);
           if constexpr (HBH) L.hbh_finish(1);
         }
-      } else if (base >= r_el && base < r_el + el_pad) {
-        const unsigned long long k = i - r_el;
-        if (k < n_el) {
+      } else if (base >= r_el && base < r_eb + eb_pad) {
+        // A chunk lies in one of the two electron ranges.
+        const bool nb = base >= r_eb;
+        const unsigned long long k = i - (nb ? r_eb : r_el);
+        if (k < (nb ? n_eb : n_el)) {
           // Up to chunk_events iterations of electron()'s tstep loop on
           // this electron; it goes back to a queue if it is still alive
           // (or if an interaction left a photon on top), to the
           // interaction queue if its step ended at a deferred interaction.
           // In the drain the interaction runs at once and the take goes on
           // with whatever electron is left on top.
-          L.take(W.el_f[bin], W.el_k[bin], static_cast<unsigned>(k), W.el_s[bin]);
+          L.take(nb ? W.eb_f[bin] : W.el_f[bin], nb ? W.eb_k[bin] : W.el_k[bin], static_cast<unsigned>(k),
+                 nb ? W.eb_s[bin] : W.el_s[bin]);
           L.pending_interaction = false;
           int n = 0;
           do {
@@ -398,7 +407,7 @@ __global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) wavefront_ke
           } while (L.alive && !L.pending_interaction && L.p.iq != 0 && ++n < (drain ? kDrainSteps : W.chunk_events));
           if (L.alive) {
             if (L.pending_interaction) L.emit_pending();
-            else L.emit(L.p);
+            else L.emit_step(L.p);
           }
           if constexpr (HBH) L.hbh_finish(1);
         }
@@ -1070,7 +1079,7 @@ omc_status run_batches(omc_engine *e, PrecisionState<R> &S, const omc_run_config
 }
 
 struct WfCounters {
-  unsigned ctr[12];
+  unsigned ctr[15];
   unsigned long long work[3];
   unsigned long long injected[2];
   unsigned bar_arrive, bar_gen;
@@ -1127,7 +1136,9 @@ omc_status run_wavefront(omc_engine *e, PrecisionState<R> &S, const omc_run_conf
   const bool hbh = cfg->history_stats != 0 && !(job && job->jobs);
   const size_t tag_bytes = (job || hbh) ? static_cast<size_t>(cap) * sizeof(int) : 0;
   size_t per_queue = static_cast<size_t>(cap) * (8 * sizeof(R) + sizeof(int)) + tag_bytes;
-  const int nqueues = 8;  // photons, electrons, electron and photon interactions; two generations each
+  // photons, electrons, electron and photon interactions, electrons near a
+  // boundary; two generations each
+  const int nqueues = 10;
   if (S.queue.ensure(nqueues * per_queue) != OMC_OK) return OMC_ERR_NOMEM;
   if (e->wf_counters.ensure(sizeof(WfCounters)) != OMC_OK) return OMC_ERR_NOMEM;
   char *qb = static_cast<char *>(S.queue.p);
@@ -1148,10 +1159,14 @@ omc_status run_wavefront(omc_engine *e, PrecisionState<R> &S, const omc_run_conf
       W.ei_f[q - 4] = f;
       W.ei_k[q - 4] = k;
       W.ei_s[q - 4] = tag;
-    } else {
+    } else if (q < 8) {
       W.pi_f[q - 6] = f;
       W.pi_k[q - 6] = k;
       W.pi_s[q - 6] = tag;
+    } else {
+      W.eb_f[q - 8] = f;
+      W.eb_k[q - 8] = k;
+      W.eb_s[q - 8] = tag;
     }
   }
   WfCounters *wc = static_cast<WfCounters *>(e->wf_counters.p);

@@ -78,6 +78,10 @@ struct EmitTargets {
   int *pi_k;
   unsigned *pi_n;
   int *pi_s;
+  R *eb_f;            // electrons within a skin depth of a boundary
+  int *eb_k;
+  unsigned *eb_n;
+  int *eb_s;
 };
 
 __device__ __forceinline__ unsigned lanemask_lt() {
@@ -100,6 +104,7 @@ struct Lane {
   bool alive;           // wavefront: p still needs to be queued
   bool defer_interactions = false;  // wavefront: queue photon and discrete electron interactions
   bool pending_interaction = false; // wavefront: p ended its step at an interaction
+  R skin = 0;           // wavefront: skin depth of p's last step (0: none, or vacuum)
   EmitTargets<R> out;   // wavefront: where this phase appends
   unsigned queue_cap;
   unsigned queue_hwm;   // highest slot appended
@@ -236,7 +241,9 @@ struct Lane {
     unsigned base = 0;
     if ((threadIdx.x & 31) == leader) base = atomicAdd(n, static_cast<unsigned>(__popc(m)));
     base = __shfl_sync(m, base, leader);
-    unsigned slot = base + __popc(m & lanemask_lt());
+    store_slot(f, k, base + __popc(m & lanemask_lt()), q, tag);
+  }
+  __device__ __forceinline__ void store_slot(R *f, int *k, unsigned slot, const Particle<R> &q, int *tag) {
     if (slot >= queue_cap) {
       err |= ERR_QUEUE;
       return;
@@ -262,6 +269,34 @@ struct Lane {
   __device__ __forceinline__ void emit(const Particle<R> &q) {
     if (q.iq == 0) emit_to(out.ph_f, out.ph_k, out.ph_n, q, out.ph_s);
     else emit_to(out.el_f, out.el_k, out.el_n, q, out.el_s);
+  }
+  // An electron after its step (or the particle left on top of its take).
+  // Electrons go to one of two queues by the kind of step they will take
+  // next, so that a warp's chunk runs one of the two branches of the step
+  // (ompmc.c:4963-5048).  Within the skin depth of a boundary (hownear <=
+  // skindepth) the step is a single-scattering step: tustep is capped at
+  // max(tperp, skindepth), so the test tustep > skindepth of the
+  // condensed-history branch fails.  The skin depth is the last step's,
+  // taken at the slightly higher energy before the step; on the 6 MV slab
+  // the guess matches the branch taken in 99.7% of the steps.  Only the
+  // order in which particles are processed changes.
+  __device__ __forceinline__ void emit_step(const Particle<R> &q) {
+    if (q.iq == 0) {
+      emit_to(out.ph_f, out.ph_k, out.ph_n, q, out.ph_s);
+      return;
+    }
+    const bool b = skin > RC(0) && hownear(q) <= skin;
+    // One append site for both queues: the lanes bound for each queue
+    // share one atomic.
+    const unsigned act = __activemask();
+    const unsigned g = __ballot_sync(act, b);
+    const unsigned m = b ? g : (act & ~g);
+    const int leader = __ffs(m) - 1;
+    unsigned base = 0;
+    if ((threadIdx.x & 31) == leader) base = atomicAdd(b ? out.eb_n : out.el_n, static_cast<unsigned>(__popc(m)));
+    base = __shfl_sync(act, base, leader);
+    store_slot(b ? out.eb_f : out.el_f, b ? out.eb_k : out.el_k, base + __popc(m & lanemask_lt()), q,
+               b ? out.eb_s : out.el_s);
   }
   // The current electron, which ended its step at a discrete interaction.
   __device__ __forceinline__ void emit_pending() { emit_to(out.ei_f, out.ei_k, out.ei_n, p, out.ei_s); }
