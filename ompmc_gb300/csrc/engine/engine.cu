@@ -29,20 +29,26 @@ namespace {
 constexpr int kBlock = 128;  // lanes per block
 // Shared memory of a block: the RANMAR states of its lanes, 3 bytes a word.
 constexpr size_t kRngSmem = static_cast<size_t>(RNG_WORDS) * kBlock * 3;
-// Blocks per SM the register budget is sized for (measured on the 6 MV
-// slab, fast-math build with one-pass electron events): FP32 5 blocks (96
-// registers) 7.96e7 hist/s, against 7.48e7 with 4 and 6.73e7 with 6 (80
-// registers and spilling); FP64 3 blocks (168 registers) 4.17e6, against
-// 4.00e6 with 2.
+// Blocks per SM the register budget is sized for, measured on the 6 MV
+// slab.  Wavefront kernel, with electrons near a boundary in their own
+// queue: FP32 5 blocks (96 registers) 8.39e7 hist/s, against 8.23e7 with
+// 4; FP64 2 blocks (248 registers) 7.04e6 at 96 particles per thread in
+// flight, against 6.88e6 with 3 blocks (168 registers) and 6.90e6 with 4
+// (128 registers, 368 bytes of spills) at the same number in flight.
+// Per-lane kernel: 5 and 3.
 #ifndef OMC_MIN_BLOCKS_FP32
 #define OMC_MIN_BLOCKS_FP32 5
 #endif
 #ifndef OMC_MIN_BLOCKS_FP64
 #define OMC_MIN_BLOCKS_FP64 3
 #endif
+#ifndef OMC_WF_MIN_BLOCKS_FP64
+#define OMC_WF_MIN_BLOCKS_FP64 2
+#endif
 template <typename R>
 struct Occupancy {
   static constexpr int kMinBlocks = sizeof(R) == 4 ? OMC_MIN_BLOCKS_FP32 : OMC_MIN_BLOCKS_FP64;
+  static constexpr int kWavefrontMinBlocks = sizeof(R) == 4 ? OMC_MIN_BLOCKS_FP32 : OMC_WF_MIN_BLOCKS_FP64;
 };
 constexpr int kDefaultDepth = 48;
 // History-by-history block pool: blocks per particle in flight, times 2.
@@ -210,7 +216,7 @@ constexpr int kDrainPerWarp = 32;
 constexpr int kDrainSteps = 4096;
 
 template <typename R>
-constexpr unsigned long long kInflightPerThread = sizeof(R) == 4 ? 128 : 64;
+constexpr unsigned long long kInflightPerThread = sizeof(R) == 4 ? 128 : 96;
 
 constexpr long long kBarrierSpinCap = 1ll << 28;  // x ~64 ns: well past any phase
 
@@ -258,7 +264,7 @@ __device__ bool grid_barrier(unsigned *arrive, unsigned *gen, unsigned nblocks,
 __device__ __forceinline__ unsigned vload(const unsigned *p) { return *static_cast<const volatile unsigned *>(p); }
 
 template <typename R, bool MULTI, bool HBH = false>
-__global__ void __launch_bounds__(kBlock, Occupancy<R>::kMinBlocks) wavefront_kernel(Params<R> P, Wavefront<R> W) {
+__global__ void __launch_bounds__(kBlock, Occupancy<R>::kWavefrontMinBlocks) wavefront_kernel(Params<R> P, Wavefront<R> W) {
   extern __shared__ unsigned char s_raw[];
   const int t = threadIdx.x;
   const int gtid = blockIdx.x * kBlock + t;
@@ -1125,8 +1131,9 @@ omc_status run_wavefront(omc_engine *e, PrecisionState<R> &S, const omc_run_conf
   const int nsplit = cfg->nsplit < 1 ? 1 : cfg->nsplit;
   const int blocks = nlanes / kBlock;
   // Particles in flight: more keeps every iteration full and amortises its
-  // grid barrier (measured on the 6 MV slab: FP32 2.77e7 / 2.85e7 / 2.95e7
-  // histories/s at 48 / 64 / 128 per thread; FP64 flat beyond 32).
+  // grid barrier (measured on the 6 MV slab: FP32 7.75e7 / 7.90e7 / 7.97e7
+  // histories/s at 32 / 64 / 128 per thread; FP64 with 2 blocks per SM
+  // 6.96e6 / 7.04e6 / 7.01e6 at 64 / 96 / 128).
   unsigned long long target = cfg->inflight > 0 ? static_cast<unsigned long long>(cfg->inflight)
                                                  : static_cast<unsigned long long>(nlanes) * kInflightPerThread<R>;
   // Worst case growth in one iteration: every photon of a cycle leaves up
