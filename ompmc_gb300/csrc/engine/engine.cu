@@ -176,12 +176,10 @@ struct Wavefront {
   R *pi_f[2];             // photons waiting for their interaction
   int *pi_k[2];
   int *pi_s[2];
-  R *eb_f[2];             // electrons within a skin depth of a boundary
-  int *eb_k[2];
-  int *eb_s[2];
   unsigned cap;           // slots per queue
   unsigned *ctr;          // [0..2] photon, [3..5] electron, [6..8] electron-interaction,
                           // [9..11] photon-interaction, [12..14] boundary-electron counters
+                          // (boundary electrons fill the electron queue from the top)
   unsigned long long *work;      // [3] chunk counters of the phase
   unsigned long long *injected;  // [2] histories injected before the iteration
   unsigned *bar_arrive;
@@ -294,11 +292,16 @@ __global__ void __launch_bounds__(kBlock, Occupancy<R>::kWavefrontMinBlocks) wav
     const int cin = it % 3, cout = (it + 1) % 3, cfree = (it + 2) % 3;
     // Everything below is read after the last barrier, so every thread
     // sees the same values and takes the same branches.
-    const unsigned n_ph = vload(W.ctr + cin);
-    const unsigned n_el = vload(W.ctr + 3 + cin);
-    const unsigned n_ei = vload(W.ctr + 6 + cin);
-    const unsigned n_pi = vload(W.ctr + 9 + cin);
-    const unsigned n_eb = vload(W.ctr + 12 + cin);
+    // A counter counts the appends that did not fit too (they set
+    // ERR_QUEUE): the reads below stay inside the queues.  The two ends of
+    // the electron queue must not have met, else records were overwritten.
+    const unsigned n_ph = min(vload(W.ctr + cin), W.cap);
+    const unsigned n_el = min(vload(W.ctr + 3 + cin), W.cap);
+    const unsigned n_ei = min(vload(W.ctr + 6 + cin), W.cap);
+    const unsigned n_pi = min(vload(W.ctr + 9 + cin), W.cap);
+    const unsigned n_eb = min(vload(W.ctr + 12 + cin), W.cap - n_el);
+    if (gtid == 0 && static_cast<unsigned long long>(vload(W.ctr + 3 + cin)) + vload(W.ctr + 12 + cin) > W.cap)
+      L.err |= ERR_QUEUE;
     const unsigned long long injected = *static_cast<volatile unsigned long long *>(W.injected + bin);
     const long long remaining = P.nhist - static_cast<long long>(injected);
     const unsigned long long inflight = static_cast<unsigned long long>(n_ph) + n_el + n_ei + n_pi + n_eb;
@@ -343,7 +346,7 @@ __global__ void __launch_bounds__(kBlock, Occupancy<R>::kWavefrontMinBlocks) wav
     L.out = EmitTargets<R>{W.ph_f[bout], W.ph_k[bout], W.ctr + cout,     W.el_f[bout], W.el_k[bout],
                            W.ctr + 3 + cout, W.ph_s[bout], W.el_s[bout],     W.ei_f[bout], W.ei_k[bout],
                            W.ctr + 6 + cout, W.ei_s[bout], W.pi_f[bout],     W.pi_k[bout], W.ctr + 9 + cout,
-                           W.pi_s[bout], W.eb_f[bout], W.eb_k[bout], W.ctr + 12 + cout, W.eb_s[bout]};
+                           W.pi_s[bout], W.ctr + 12 + cout};
     // Chunk ranges of the phase in claim order [new histories | photon
     // flights | photon interactions | electron steps | electron steps near
     // a boundary | electron interactions], each padded to a multiple of 32
@@ -399,8 +402,8 @@ __global__ void __launch_bounds__(kBlock, Occupancy<R>::kWavefrontMinBlocks) wav
           // interaction queue if its step ended at a deferred interaction.
           // In the drain the interaction runs at once and the take goes on
           // with whatever electron is left on top.
-          L.take(nb ? W.eb_f[bin] : W.el_f[bin], nb ? W.eb_k[bin] : W.el_k[bin], static_cast<unsigned>(k),
-                 nb ? W.eb_s[bin] : W.el_s[bin]);
+          L.take(W.el_f[bin], W.el_k[bin], nb ? W.cap - 1 - static_cast<unsigned>(k) : static_cast<unsigned>(k),
+                 W.el_s[bin]);
           L.pending_interaction = false;
           int n = 0;
           do {
@@ -1143,9 +1146,9 @@ omc_status run_wavefront(omc_engine *e, PrecisionState<R> &S, const omc_run_conf
   const bool hbh = cfg->history_stats != 0 && !(job && job->jobs);
   const size_t tag_bytes = (job || hbh) ? static_cast<size_t>(cap) * sizeof(int) : 0;
   size_t per_queue = static_cast<size_t>(cap) * (8 * sizeof(R) + sizeof(int)) + tag_bytes;
-  // photons, electrons, electron and photon interactions, electrons near a
-  // boundary; two generations each
-  const int nqueues = 10;
+  // photons, electrons (those near a boundary from the top), electron and
+  // photon interactions; two generations each
+  const int nqueues = 8;
   if (S.queue.ensure(nqueues * per_queue) != OMC_OK) return OMC_ERR_NOMEM;
   if (e->wf_counters.ensure(sizeof(WfCounters)) != OMC_OK) return OMC_ERR_NOMEM;
   char *qb = static_cast<char *>(S.queue.p);
@@ -1166,14 +1169,10 @@ omc_status run_wavefront(omc_engine *e, PrecisionState<R> &S, const omc_run_conf
       W.ei_f[q - 4] = f;
       W.ei_k[q - 4] = k;
       W.ei_s[q - 4] = tag;
-    } else if (q < 8) {
+    } else {
       W.pi_f[q - 6] = f;
       W.pi_k[q - 6] = k;
       W.pi_s[q - 6] = tag;
-    } else {
-      W.eb_f[q - 8] = f;
-      W.eb_k[q - 8] = k;
-      W.eb_s[q - 8] = tag;
     }
   }
   WfCounters *wc = static_cast<WfCounters *>(e->wf_counters.p);

@@ -78,10 +78,8 @@ struct EmitTargets {
   int *pi_k;
   unsigned *pi_n;
   int *pi_s;
-  R *eb_f;            // electrons within a skin depth of a boundary
-  int *eb_k;
-  unsigned *eb_n;
-  int *eb_s;
+  unsigned *eb_n;     // electrons within a skin depth of a boundary: the
+                      // electron queue's slots counted down from the top
 };
 
 __device__ __forceinline__ unsigned lanemask_lt() {
@@ -241,14 +239,15 @@ struct Lane {
     unsigned base = 0;
     if ((threadIdx.x & 31) == leader) base = atomicAdd(n, static_cast<unsigned>(__popc(m)));
     base = __shfl_sync(m, base, leader);
-    store_slot(f, k, base + __popc(m & lanemask_lt()), q, tag);
-  }
-  __device__ __forceinline__ void store_slot(R *f, int *k, unsigned slot, const Particle<R> &q, int *tag) {
+    const unsigned slot = base + __popc(m & lanemask_lt());
     if (slot >= queue_cap) {
       err |= ERR_QUEUE;
       return;
     }
     if (slot > queue_hwm) queue_hwm = slot;
+    store_slot(f, k, slot, q, tag);
+  }
+  __device__ __forceinline__ void store_slot(R *f, int *k, unsigned slot, const Particle<R> &q, int *tag) {
     size_t c = queue_cap;
     __stcg(f + slot, q.e);
     __stcg(f + c + slot, q.x);
@@ -279,7 +278,9 @@ struct Lane {
   // condensed-history branch fails.  The skin depth is the last step's,
   // taken at the slightly higher energy before the step; on the 6 MV slab
   // the guess matches the branch taken in 99.7% of the steps.  Only the
-  // order in which particles are processed changes.
+  // order in which particles are processed changes.  The two share one
+  // buffer: the others fill it from slot 0 up, the boundary electrons from
+  // the top down, so together they have the one queue's worst-case room.
   __device__ __forceinline__ void emit_step(const Particle<R> &q) {
     if (q.iq == 0) {
       emit_to(out.ph_f, out.ph_k, out.ph_n, q, out.ph_s);
@@ -295,8 +296,13 @@ struct Lane {
     unsigned base = 0;
     if ((threadIdx.x & 31) == leader) base = atomicAdd(b ? out.eb_n : out.el_n, static_cast<unsigned>(__popc(m)));
     base = __shfl_sync(act, base, leader);
-    store_slot(b ? out.eb_f : out.el_f, b ? out.eb_k : out.el_k, base + __popc(m & lanemask_lt()), q,
-               b ? out.eb_s : out.el_s);
+    const unsigned idx = base + __popc(m & lanemask_lt());
+    if (idx >= queue_cap) {
+      err |= ERR_QUEUE;
+      return;
+    }
+    if (idx > queue_hwm) queue_hwm = idx;
+    store_slot(out.el_f, out.el_k, b ? queue_cap - 1 - idx : idx, q, out.el_s);
   }
   // The current electron, which ended its step at a discrete interaction.
   __device__ __forceinline__ void emit_pending() { emit_to(out.ei_f, out.ei_k, out.ei_n, p, out.ei_s); }
