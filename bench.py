@@ -748,7 +748,8 @@ def run_serve_leg(args, local_rank):
         for mode, max_jobs, policy in modes:
             if wanted and mode not in wanted:
                 continue
-            srv = api.Server(media, data_text, precision=api.FP32, max_jobs=max_jobs, policy=policy)
+            srv = api.Server(media, data_text, precision=api.FP32, max_jobs=max_jobs, policy=policy,
+                             round_histories=getattr(args, "serve_round_histories", 0))
             # warm-up job (tables, kernels)
             srv.wait(srv.submit(phs[0], sources.get((0, 0)) or api.build_source(inputs[0], phs[0]), 0.7, 0.01,
                                 1000, 10))
@@ -780,7 +781,9 @@ def run_serve_leg(args, local_rank):
                 "dtype": "f32", "config": {"workload": SERVE_WORKLOAD, "jobs": njobs, "rate_per_s": args.serve_rate,
                                            "mean_histories": mean_h, "total_histories": total,
                                            "beamlet_jobs": int(sum(d[3] is not None for d in draws)),
-                                           "seed": args.serve_seed},
+                                           "seed": args.serve_seed,
+                                           "round_histories": getattr(args, "serve_round_histories", 0) or
+                                           "adaptive: a quarter of the resident backlog, 4e6 to 3.2e7"},
                 "continuous": out.get("continuous"), "continuous_equal_shares": out.get("continuous_equal_shares"),
                 "one_at_a_time": out.get("one_at_a_time")}
 
@@ -831,6 +834,10 @@ def main():
     ap.add_argument("--serve-max-histories", type=float, default=1e8)
     ap.add_argument("--serve-seed", type=int, default=5)
     ap.add_argument("--serve-beamlet-frac", type=float, default=0.25, help="share of beamlet (dij) jobs in the mix")
+    ap.add_argument("--serve-round-histories", type=int, default=0,
+                    help="histories per server round (0: adaptive to the resident backlog)")
+    ap.add_argument("--serve-modes", type=lambda v: tuple(v.split(",")), default=None,
+                    help="comma list of continuous, continuous_equal_shares, one_at_a_time (default: all)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -588,7 +588,10 @@ typedef struct omc_server_config {
                                    the free memory at creation            */
     int max_jobs;               /* resident jobs at most; 0 = 256          */
     long long round_histories;  /* histories per round over all resident
-                                   jobs; 0 = 4,000,000                     */
+                                   jobs; 0 = adaptive: 4e6 while more than
+                                   two jobs are resident, else a quarter of
+                                   their histories left, at most 4x the
+                                   shortest job's, within [4e6, 3.2e7]     */
     int nsplit;                 /* photon splitting, every job (0 = 1)     */
     int ixx, jxx;               /* RANMAR seeds of the server's streams    */
     int policy;                 /* round quotas: OMC_SERVE_SHORTEST_FIRST

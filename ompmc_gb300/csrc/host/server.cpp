@@ -85,6 +85,7 @@ struct omc_server {
   long long next_id = 1;
   long long resident_bytes = 0;
   bool stop = false;
+  bool adaptive_rounds = false;  // round_histories chosen per round
   omc_server_stats st{};
   std::thread admit_thread, sched_thread;
 
@@ -92,6 +93,11 @@ struct omc_server {
 };
 
 namespace {
+
+// Round size bounds of the adaptive rounds (round_histories = 0).
+constexpr long long kRoundMin = 4000000;
+constexpr long long kRoundMax = 32000000;
+constexpr size_t kFewJobs = 2;
 
 // A job's phantom with its media renumbered onto the server's, and its
 // regions against the server's tables (initRegions, omc_regions_build).
@@ -181,9 +187,29 @@ void scheduler_loop(omc_server *s) {
     std::vector<std::shared_ptr<Job>> all = s->resident;
     lk.unlock();
     std::vector<std::shared_ptr<Job>> round = all;  // field and beamlet jobs alike
-    const long long R = s->cfg.round_histories;
     std::vector<long long> left(round.size()), quota(round.size(), 0);
-    for (size_t i = 0; i < round.size(); i++) left[i] = omc_job_histories(round[i]->dev) - omc_job_done(round[i]->dev);
+    long long backlog = 0, shortest = -1;
+    for (size_t i = 0; i < round.size(); i++) {
+      left[i] = omc_job_histories(round[i]->dev) - omc_job_done(round[i]->dev);
+      backlog += left[i];
+      if (left[i] > 0 && (shortest < 0 || left[i] < shortest)) shortest = left[i];
+    }
+    long long R = s->cfg.round_histories;
+    if (s->adaptive_rounds) {
+      // A round ends with a tail in which its last histories finish at low
+      // occupancy (about 40 ms on a GB300, whatever the round's size), so
+      // short rounds cost throughput and long ones make arrivals and small
+      // jobs wait.  While few jobs are resident (a lightly loaded server)
+      // a round takes a quarter of the backlog, but at most four times the
+      // histories the shortest job has left, between kRoundMin and
+      // kRoundMax; with more jobs resident, kRoundMin, so that the small
+      // ones among them and new arrivals pass the large ones soon.
+      R = kRoundMin;
+      if (round.size() <= kFewJobs) {
+        R = std::min(backlog / 4, 4 * std::max(shortest, 0ll));
+        R = std::min(kRoundMax, std::max(kRoundMin, R));
+      }
+    }
     long long budget = R;
     if (s->cfg.policy == OMC_SERVE_EQUAL_SHARES) {
       // Equal shares; a job with fewer histories left takes only those and
@@ -287,7 +313,7 @@ extern "C" omc_status omc_server_create(const omc_server_config *cfg, const omc_
   std::unique_ptr<omc_server> s(new omc_server());
   s->cfg = *cfg;
   if (s->cfg.max_jobs <= 0) s->cfg.max_jobs = 256;
-  if (s->cfg.round_histories <= 0) s->cfg.round_histories = 4000000;
+  s->adaptive_rounds = s->cfg.round_histories <= 0;
   if (s->cfg.nsplit <= 0) s->cfg.nsplit = 1;
   char names[OMC_MXMED][OMC_NAME_LEN];
   std::memset(names, 0, sizeof names);
