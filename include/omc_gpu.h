@@ -667,6 +667,12 @@ typedef struct omc_server_stats {
 } omc_server_stats;
 
 omc_status omc_server_get_stats(omc_server *s, omc_server_stats *st);
+/* Histories of the next round, as the scheduler picks them: `configured`
+ * (round_histories) when > 0; else the adaptive size from the resident
+ * jobs' histories left (`backlog`), the fewest any of them has left
+ * (`shortest`) and their number (`resident`).  Host only. */
+long long omc_server_round_histories(long long configured, long long backlog, long long shortest,
+                                     int resident);
 /* Stops both threads after the current round; queued jobs are dropped. */
 void omc_server_destroy(omc_server *s);
 

@@ -201,6 +201,7 @@ def lib(path: str | None = None):
         "omc_server_wait_dij": ([vp, C.c_longlong, C.c_double, pp(pp(Dij_t)), pp(ServerResult_t)], C.c_int),
         "omc_server_get_stats": ([vp, pp(ServerStats_t)], C.c_int),
         "omc_server_destroy": ([vp], None),
+        "omc_server_round_histories": ([C.c_longlong, C.c_longlong, C.c_longlong, C.c_int], C.c_longlong),
         "omc_engine_tune": ([vp, pp(RunConfig_t), C.c_longlong, pp(RunConfig_t), pp(C.c_double)], C.c_int),
         "omc_engine_trace": ([vp, C.c_int], C.c_int),
         "omc_engine_trace_read": ([vp, pp(C.c_longlong), C.c_int, pp(C.c_int)], C.c_int),

@@ -194,22 +194,8 @@ void scheduler_loop(omc_server *s) {
       backlog += left[i];
       if (left[i] > 0 && (shortest < 0 || left[i] < shortest)) shortest = left[i];
     }
-    long long R = s->cfg.round_histories;
-    if (s->adaptive_rounds) {
-      // A round ends with a tail in which its last histories finish at low
-      // occupancy (about 40 ms on a GB300, whatever the round's size), so
-      // short rounds cost throughput and long ones make arrivals and small
-      // jobs wait.  While few jobs are resident (a lightly loaded server)
-      // a round takes a quarter of the backlog, but at most four times the
-      // histories the shortest job has left, between kRoundMin and
-      // kRoundMax; with more jobs resident, kRoundMin, so that the small
-      // ones among them and new arrivals pass the large ones soon.
-      R = kRoundMin;
-      if (round.size() <= kFewJobs) {
-        R = std::min(backlog / 4, 4 * std::max(shortest, 0ll));
-        R = std::min(kRoundMax, std::max(kRoundMin, R));
-      }
-    }
+    const long long R = omc_server_round_histories(s->adaptive_rounds ? 0 : s->cfg.round_histories, backlog,
+                                                   shortest, static_cast<int>(round.size()));
     long long budget = R;
     if (s->cfg.policy == OMC_SERVE_EQUAL_SHARES) {
       // Equal shares; a job with fewer histories left takes only those and
@@ -303,6 +289,22 @@ void scheduler_loop(omc_server *s) {
 }
 
 }  // namespace
+
+// A round ends with a tail in which its last histories finish at low
+// occupancy (about 40 ms on a GB300, whatever the round's size), so short
+// rounds cost throughput and long ones make arrivals and small jobs wait.
+// While few jobs are resident (a lightly loaded server) a round takes a
+// quarter of the backlog, but at most four times the histories the
+// shortest job has left, between kRoundMin and kRoundMax; with more jobs
+// resident, kRoundMin, so that the small ones among them and new arrivals
+// pass the large ones soon.
+extern "C" long long omc_server_round_histories(long long configured, long long backlog, long long shortest,
+                                                int resident) {
+  if (configured > 0) return configured;
+  if (resident > static_cast<int>(kFewJobs)) return kRoundMin;
+  const long long r = std::min(backlog / 4, 4 * std::max(shortest, 0ll));
+  return std::min(kRoundMax, std::max(kRoundMin, r));
+}
 
 extern "C" omc_status omc_server_create(const omc_server_config *cfg, const omc_input *data_keys, int nmed,
                                         const char *const *media, omc_server **out) {

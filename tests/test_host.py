@@ -278,3 +278,21 @@ def test_3ddose_text_is_printf_byte_for_byte(native, tmp_path, problem_factory):
     assert lines[0] == "%5d%5d%5d" % (s.nx, s.ny, s.nz)
     assert lines[4] == "".join("%e " % x for x in d[1:])
     assert lines[5] == "".join("%f " % x for x in u[1:])
+
+
+def test_server_round_size_rule(native):
+    """The dose server's round size: a configured size as given; else 4e6
+    while more than two jobs are resident, and with one or two a quarter of
+    their histories left, at most four times the shortest job's, within
+    [4e6, 3.2e7]."""
+    from ompmc_gb300 import _native as N
+
+    f = N.lib().omc_server_round_histories
+    assert f(150000, 10**9, 10**5, 1) == 150000
+    assert f(0, 10**9, 10**8, 3) == 4_000_000              # busy: short rounds
+    assert f(0, 10**8, 10**8, 1) == 25_000_000             # one large job: a quarter of it
+    assert f(0, 10**9, 10**9, 2) == 32_000_000             # capped
+    assert f(0, 10**8 + 10**6, 10**6, 2) == 4_000_000      # a small job resident: 4x its rest, at least 4e6
+    assert f(0, 6 * 10**7, 3 * 10**6, 2) == 12_000_000
+    assert f(0, 10**5, 10**5, 1) == 4_000_000              # floor
+    assert f(0, 0, -1, 0) == 4_000_000
