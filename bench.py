@@ -609,6 +609,35 @@ def run_vrt_leg(args, local_rank):
             "results": out}
 
 
+def run_queue_traffic_leg(args, local_rank):
+    """Four one-launch FP32 jobs of 1e7 histories on the benchmark workload
+    that separate the two large working sets of the wavefront kernel: one or
+    ten batch tallies (27 or 270 MB) times 2e5 or 2e6 particles in flight
+    (one queue generation of 7 or 72 MB).  Run under ncu with DRAM counters
+    (-k regex:wavefront_kernel -s 1 -c 4) it gives the DRAM bytes of each;
+    alone it prints the launch times."""
+    import torch
+
+    from ompmc_gb300 import api
+
+    torch.cuda.set_device(local_rank)
+    out = []
+    with tempfile.TemporaryDirectory() as tmp:
+        prob = build_problem(tmp)
+        eng = api.Engine(local_rank).load(prob)
+        eng.run(nperbatch=1_000_000, nbatch=1, precision=api.FP32, inflight=200_000)  # warm-up launch
+        for nb, inflight in ((1, 200_000), (1, 2_000_000), (10, 200_000), (10, 2_000_000)):
+            a, a2, st = eng.run(nperbatch=10_000_000 // nb, nbatch=nb, precision=api.FP32, continue_streams=1,
+                                inflight=inflight)
+            if st.error_flags:
+                raise RuntimeError(f"device error flags {st.error_flags:#x}")
+            out.append({"nbatch": nb, "inflight": inflight, "kernel_ms": st.kernel_ms,
+                        "histories_per_s": 1e7 / (st.kernel_ms / 1e3)})
+        eng.close()
+    return {"metric": "wavefront launch time by tally and queue working set", "n_gpus": 1, "data": "synthetic",
+            "config": {"workload": WORKLOAD, "histories": 10_000_000}, "results": out}
+
+
 CT_WORKLOAD = ("CT-like blob phantom 256x256x128 @ 2 mm (seed 2024), synthetic 6 MV, point source SSD 100 cm; "
                "fields 3x3 and 10x10 cm2 at gantry 0 (+z) and gantry 90 (phantom axes x and z exchanged so that "
                "the beam enters along +z)")
@@ -827,6 +856,8 @@ def main():
     ap.add_argument("--serve", action="store_true", help="measure the dose-server mix instead (one JSON line)")
     ap.add_argument("--ct", action="store_true", help="FP32-vs-FP64 dose error per field on the CT-like phantom")
     ap.add_argument("--vrt", action="store_true", help="efficiency 1/(s^2 T) against the photon splitting number")
+    ap.add_argument("--queue-traffic", action="store_true",
+                    help="four one-launch jobs that separate the tally and queue working sets (for a DRAM capture)")
     ap.add_argument("--vrt-histories", type=int, default=2_000_000, help="histories per batch (10 batches)")
     ap.add_argument("--ct-histories", type=int, default=20_000_000)
     ap.add_argument("--serve-jobs", type=int, default=40)
@@ -858,6 +889,10 @@ def main():
     if args.ct:
         if rank == 0:
             print(json.dumps(run_ct_leg(args, local_rank)), flush=True)
+        return
+    if args.queue_traffic:
+        if rank == 0:
+            print(json.dumps(run_queue_traffic_leg(args, local_rank)), flush=True)
         return
     if args.serve:
         if rank == 0:
