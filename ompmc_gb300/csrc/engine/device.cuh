@@ -38,6 +38,9 @@ enum : unsigned {
 // flag instead of a hung GPU.
 constexpr int kRejectCap = 1 << 20;
 constexpr long long kEventCap = 1ll << 22;
+// A photon flight with no crossing cap (split photons, the per-lane
+// schedule, the end-of-run drain).
+constexpr int kNoFlightCap = 1 << 30;
 
 // ---------------------------------------------------------------------------
 // Particles.  dnear is not carried: the reference writes it but never reads

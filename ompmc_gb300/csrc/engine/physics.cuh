@@ -80,6 +80,7 @@ struct EmitTargets {
   int *pi_s;
   unsigned *eb_n;     // electrons within a skin depth of a boundary: the
                       // electron queue's slots counted down from the top
+  R *ph_t;            // photon flights: mean free paths left (-1: a new flight)
 };
 
 __device__ __forceinline__ unsigned lanemask_lt() {
@@ -103,6 +104,9 @@ struct Lane {
   bool defer_interactions = false;  // wavefront: queue photon and discrete electron interactions
   bool pending_interaction = false; // wavefront: p ended its step at an interaction
   R skin = 0;           // wavefront: skin depth of p's last step (0: none, or vacuum)
+  R cont_mfp = -1;      // wavefront: mean free paths left of the photon emitted (-1: a new flight)
+  R taken_mfp = -1;     // wavefront: mean free paths left of the photon taken (-1: a new flight)
+  int flight_cap = kNoFlightCap;  // wavefront: voxel crossings of a photon flight per event
   EmitTargets<R> out;   // wavefront: where this phase appends
   unsigned queue_cap;
   unsigned queue_hwm;   // highest slot appended
@@ -266,8 +270,25 @@ struct Lane {
     }
   }
   __device__ __forceinline__ void emit(const Particle<R> &q) {
-    if (q.iq == 0) emit_to(out.ph_f, out.ph_k, out.ph_n, q, out.ph_s);
+    if (q.iq == 0) emit_photon(q);
     else emit_to(out.el_f, out.el_k, out.el_n, q, out.el_s);
+  }
+  // A photon to the flight queue, with the mean free paths its flight has
+  // left (cont_mfp; -1 for a new flight).
+  __device__ __forceinline__ void emit_photon(const Particle<R> &q) {
+    unsigned m = __activemask();
+    int leader = __ffs(m) - 1;
+    unsigned base = 0;
+    if ((threadIdx.x & 31) == leader) base = atomicAdd(out.ph_n, static_cast<unsigned>(__popc(m)));
+    base = __shfl_sync(m, base, leader);
+    const unsigned slot = base + __popc(m & lanemask_lt());
+    if (slot >= queue_cap) {
+      err |= ERR_QUEUE;
+      return;
+    }
+    if (slot > queue_hwm) queue_hwm = slot;
+    store_slot(out.ph_f, out.ph_k, slot, q, out.ph_s);
+    __stcg(out.ph_t + slot, cont_mfp);
   }
   // An electron after its step (or the particle left on top of its take).
   // Electrons go to one of two queues by the kind of step they will take
@@ -283,7 +304,7 @@ struct Lane {
   // the top down, so together they have the one queue's worst-case room.
   __device__ __forceinline__ void emit_step(const Particle<R> &q) {
     if (q.iq == 0) {
-      emit_to(out.ph_f, out.ph_k, out.ph_n, q, out.ph_s);
+      emit_photon(q);
       return;
     }
     const bool b = skin > RC(0) && hownear(q) <= skin;
