@@ -31,7 +31,8 @@ constexpr int kBlock = 128;  // lanes per block
 constexpr size_t kRngSmem = static_cast<size_t>(RNG_WORDS) * kBlock * 3;
 // Blocks per SM the register budget is sized for, measured on the 6 MV
 // slab.  Wavefront kernel, with electrons near a boundary in their own
-// queue: FP32 5 blocks (96 registers) 8.39e7 hist/s, against 8.23e7 with
+// queue (before the photon flight cap): FP32 5 blocks (96 registers)
+// 8.39e7 hist/s, against 8.23e7 with
 // 4; FP64 2 blocks (248 registers) 7.04e6 at 96 particles per thread in
 // flight, against 6.88e6 with 3 blocks (168 registers) and 6.90e6 with 4
 // (128 registers, 368 bytes of spills) at the same number in flight.
