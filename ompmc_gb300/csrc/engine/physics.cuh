@@ -236,8 +236,11 @@ struct Lane {
   }
 
   // Wavefront append: lanes that emit together share one atomic per queue
-  // (ballot + popc), so a warp writes consecutive, coalesced slots.
-  __device__ __forceinline__ void emit_to(R *f, int *k, unsigned *n, const Particle<R> &q, int *tag) {
+  // (ballot + popc), so a warp writes consecutive, coalesced slots.  mfp
+  // (the photon flight queue only): where the mean free paths the flight
+  // has left go (cont_mfp; -1 for a new flight).
+  __device__ __forceinline__ void emit_to(R *f, int *k, unsigned *n, const Particle<R> &q, int *tag,
+                                          R *mfp = nullptr) {
     unsigned m = __activemask();
     int leader = __ffs(m) - 1;
     unsigned base = 0;
@@ -250,6 +253,7 @@ struct Lane {
     }
     if (slot > queue_hwm) queue_hwm = slot;
     store_slot(f, k, slot, q, tag);
+    if (mfp) __stcg(mfp + slot, cont_mfp);
   }
   __device__ __forceinline__ void store_slot(R *f, int *k, unsigned slot, const Particle<R> &q, int *tag) {
     size_t c = queue_cap;
@@ -276,19 +280,7 @@ struct Lane {
   // A photon to the flight queue, with the mean free paths its flight has
   // left (cont_mfp; -1 for a new flight).
   __device__ __forceinline__ void emit_photon(const Particle<R> &q) {
-    unsigned m = __activemask();
-    int leader = __ffs(m) - 1;
-    unsigned base = 0;
-    if ((threadIdx.x & 31) == leader) base = atomicAdd(out.ph_n, static_cast<unsigned>(__popc(m)));
-    base = __shfl_sync(m, base, leader);
-    const unsigned slot = base + __popc(m & lanemask_lt());
-    if (slot >= queue_cap) {
-      err |= ERR_QUEUE;
-      return;
-    }
-    if (slot > queue_hwm) queue_hwm = slot;
-    store_slot(out.ph_f, out.ph_k, slot, q, out.ph_s);
-    __stcg(out.ph_t + slot, cont_mfp);
+    emit_to(out.ph_f, out.ph_k, out.ph_n, q, out.ph_s, out.ph_t);
   }
   // An electron after its step (or the particle left on top of its take).
   // Electrons go to one of two queues by the kind of step they will take
